@@ -1,0 +1,397 @@
+#!/usr/bin/env python3
+"""Benchmark of the photon-transport hot path on one GB300.
+
+Workload (default, `--config c1`): the 400-module detector, one isotropic
+point emitter inside the hull, 1e8 photons, Frank-Tamm spectrum on 300-800 nm,
+Cascadia water, seeds 1..5 (one emitter position per seed; step k uses seed
+1 + k % 5).  A "step" is one propagation of all 1e8 photons.
+
+  value  photons/s of the propagation kernel, device-resident inputs, timed with
+         CUDA events on the launching stream (L2 flushed between steps by
+         writing a 512 MiB buffer).
+  e2e    photons/s through the public API call a user makes
+         (propagate_photons(setup, hit_buffers)): source upload, kernel,
+         counters and the hit rows copied back to host memory, hit table built.
+  roofline  FP32-issue bound: algorithmic FLOPs of the photon steps taken
+         (device counter) / kernel time against a measured FFMA peak.
+  cpu_baseline  the CPU oracle (a C restatement of the reference's step
+         functions, all host threads) on a bounded sample of the same workload.
+
+`--impl reference` times the reference algorithm on the host cores (the
+oracle: the reference itself is Julia/CUDA.jl and is not runnable here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as entry  # noqa: E402
+
+# Algorithmic FP32 operations of one photon step with ONE candidate sphere
+# test, counted from the oracle's step body (oracle/pp_oracle_body.inc):
+#   step length -log(u)*L .......................... 2 (log counted as 1)
+#   ray-sphere test (3 sub, 2 dot3 = 10, b: 3, sqrt 1, d: 1, 2 compares) 20
+#   position update 3 FMA ........................... 6
+#   path length (+ Kahan 3) and time ................ 6
+#   phase function: HG 8, ES 10 + 2 cbrt, mixture 1 .. 21
+#   sin(theta) 3, phi 1, sincos 2, new dir 2 ......... 8
+#   rotation from e_z (Rodrigues form) ............... 19
+FLOPS_PER_STEP = 82
+
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "propagate_kernel_c1.txt")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--photons", type=float, default=None)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_setups(pp, config, photons, n_seeds=5):
+    if config == "c0":
+        out = [pp.workloads.c0_setup(photons, seed=s) for s in range(1, n_seeds + 1)]
+    else:
+        out = [pp.workloads.c1_setup(photons=photons, seed=s) for s in range(1, n_seeds + 1)]
+    # one detector, medium and spectrum shared by all seeds (uploaded once)
+    for s in out[1:]:
+        s.targets, s.medium, s.spec_dist = out[0].targets, out[0].medium, out[0].spec_dist
+        s.spectrum_knots = out[0].spectrum_knots
+    return out
+
+
+def shard_sources(setup, rank, world):
+    """Photons of each source split into contiguous ranges, one per rank; the
+    Philox streams are keyed on the photon index, so the union of the shards is
+    the single-GPU run."""
+    import copy
+    from importlib import import_module
+    pp = import_module(entry.PKG_NAME)
+    out = []
+    for s in setup.sources:
+        n = pp.source_photons(s.photons, setup.photon_scaling)
+        lo, hi = n * rank // world, n * (rank + 1) // world
+        c = copy.copy(s)
+        c.photons = hi - lo
+        c.first_photon = lo
+        out.append(c)
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self._proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for n, v in zip(names, s[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def profile_traffic():
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    try:
+        text = open(PROFILE_SUMMARY).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch_full:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+def cpu_baseline(pp, orc, config, seconds, photons_full):
+    """The oracle (FP32, all host threads) on a bounded sample of the workload."""
+    setup = make_setups(pp, config, photons_full, n_seeds=1)[0]
+    nthreads = int(orc.load().ppo_max_threads())
+    run = orc.Run.from_setup(setup)
+    n_cal = 4000
+    t0 = time.perf_counter()
+    run.propagate(0, 0, n_cal, nthreads=nthreads, capacity=n_cal)
+    dt = time.perf_counter() - t0
+    rate0 = n_cal / max(dt, 1e-6)
+    # the sample is the first n photons of the seed-1 source
+    n = int(min(photons_full, max(n_cal, rate0 * seconds)))
+    t0 = time.perf_counter()
+    hits, st = run.propagate(0, 0, n, nthreads=nthreads, capacity=n)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "photons/s", "cores": nthreads, "kind": "port",
+            "sample": f"first {n} photons of the seed-1 {config.upper()} source, "
+                      f"{len(hits)} hits, {dt:.1f} s"}
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm (oracle port) on host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    pp = entry.load()
+    orc = entry.load_oracle()
+    orc.build()
+    photons = int(args.photons or (1e8 if args.config == "c1" else 1e5))
+    nthreads = int(orc.load().ppo_max_threads())
+    setups = make_setups(pp, args.config, photons)
+    runs = [orc.Run.from_setup(s) for s in setups]
+    # size one step's sample to ~1/(steps+warmup) of a ~3 minute budget
+    t0 = time.perf_counter()
+    runs[0].propagate(0, 0, 2000, nthreads=nthreads, capacity=2000)
+    rate = 2000 / max(time.perf_counter() - t0, 1e-6)
+    per_step = max(2000, min(photons, int(rate * 150.0 / max(1, args.steps + args.warmup))))
+    for k in range(args.warmup):
+        runs[k % 5].propagate(0, 0, min(per_step, 2000), nthreads=nthreads, capacity=per_step)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        runs[k % 5].propagate(0, 0, per_step, nthreads=nthreads, capacity=per_step)
+    dt = time.perf_counter() - t0
+    value = per_step * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "photons/s on 1 GB300", "value": value,
+        "unit": "photons/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.config.upper()}: reference algorithm (CPU oracle port; "
+                               "PhotonPropagation.jl/CUDA.jl is not runnable on this box)",
+                   "photons_per_step_sample": per_step, "photons_full": photons},
+        "cpu_baseline": {"value": value, "unit": "photons/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{per_step} photons per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": "photons/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    pp = entry.load()
+    photons = int(args.photons or (1e8 if args.config == "c1" else 1e5))
+    setups = make_setups(pp, args.config, photons)
+    ctxs = []
+    for s in setups:
+        c = pp.Context(local)
+        s.upload(c)
+        srcs = shard_sources(s, rank, world) if world > 1 else s.sources
+        from importlib import import_module
+        recs = import_module(entry.PKG_NAME).sources.to_records(srcs)
+        c.set_sources(recs, len(srcs), s.photon_scaling)
+        c._recs = recs
+        ctxs.append(c)
+    tuning = None
+    if not args.no_autotune:
+        t, rate = ctxs[0].autotune(setups[0].seed, 15, sample_photons=min(photons, 8_000_000))
+        tuning = dict(block_threads=t.block_threads, photons_per_thread=t.photons_per_thread,
+                      cell_size=t.cell_size)
+        for c in ctxs[1:]:
+            c.set_tuning(**tuning)
+    photons_rank = ctxs[0].total_photons()
+
+    cap = max(1_000_000, photons_rank // 20)
+    hits = torch.empty(cap * 80, dtype=torch.uint8, device="cuda")
+    counters = torch.zeros(len(ctxs) * 64, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+
+    def launch(k):
+        c = ctxs[k % len(ctxs)]
+        c.launch(setups[k % len(ctxs)].seed, 15, hits.data_ptr(), cap,
+                 counters.data_ptr() + 64 * (k % len(ctxs)), stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            flush.zero_()
+            launch(k)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    steps_taken = 0
+    n_hits_total = 0
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            launch(k)
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        torch.distributed.barrier()
+    clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    cnt = counters.cpu().numpy().view(np.uint64).reshape(len(ctxs), 8)
+    for k in range(args.steps):
+        row = cnt[k % len(ctxs)]
+        steps_taken += int(row[2])
+        n_hits_total += int(row[0])
+        assert int(row[4]) & 0xffffffff == 0, f"device error flags {row[4]}"
+        assert int(row[1]) == photons_rank, (int(row[1]), photons_rank)
+    kernel_s = sum(ms) / 1e3
+    if world > 1:
+        t = torch.tensor([kernel_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        kernel_s = float(t.item())
+    value = photons_rank * world * args.steps / kernel_s
+    ms_per_step = kernel_s * 1e3 / args.steps
+
+    # roofline: FP32-issue bound
+    peak = pp.measure_fp32_peak(local)
+    # the photon steps of the last timed steps (counters of each context)
+    flops = FLOPS_PER_STEP * steps_taken
+    achieved = flops / kernel_s / 1e12
+    traffic_full = profile_traffic()
+
+    # e2e through the public API with host buffers
+    e2e_steps = args.e2e_steps or min(args.steps, 3)
+    hb = pp.HitBuffers(cap, local)
+    for s in setups:
+        if world > 1:
+            s.sources = shard_sources(s, rank, world)
+    pp.propagate_photons(setups[0], hb)  # warm (uploads this setup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    e2e_photons = 0
+    for k in range(e2e_steps):
+        s = setups[k % len(setups)]
+        t = pp.propagate_photons(s, hb)
+        e2e_photons += sum(pp.source_photons(x.photons, s.photon_scaling) for x in s.sources)
+        h2d += 96 * len(s.sources) + 24 * len(s.sources) + 8
+        d2h += 48 + 80 * t.nrow
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_photons * world / e2e_s
+
+    if rank != 0:
+        return 0
+    orc = entry.load_oracle()
+    orc.build()
+    base = cpu_baseline(pp, orc, args.config, args.cpu_seconds, photons)
+    tun = ctxs[0].get_tuning()
+    gi = ctxs[0].grid_info()
+    line = {
+        "metric": "photons/s on 1 GB300", "value": value, "unit": "photons/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {
+            "workload": ("C1: 400 spheres r=0.2159 m on 20 strings (x,y ~ U(-250,250), "
+                         "z=-250..225 step 25), isotropic point in the hull, 1e8 photons, "
+                         "Frank-Tamm 300-800 nm, Cascadia water, 15 steps, seeds 1-5")
+            if args.config == "c1" else "C0: README single-module example",
+            "photons_per_step": photons, "seeds": [1, 2, 3, 4, 5],
+            "l2": "flushed between steps (512 MiB write)",
+            "tuning": {"block_threads": tun.block_threads,
+                       "photons_per_thread": tun.photons_per_thread,
+                       "cell_size_m": round(float(tun.cell_size or gi["cell"][0]), 3),
+                       "grid_cells": gi["dims"], "autotuned": tuning is not None},
+            "parallelism": f"photon-range shards x{world}" if world > 1 else "single GPU",
+        },
+        "e2e": {"value": e2e_value, "unit": "photons/s", "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
+                "api": "propagate_photons(setup, hit_buffers) -> hit table in host memory"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak,
+                     "traffic": traffic_full,
+                     "note": f"{FLOPS_PER_STEP} algorithmic FP32 ops per photon step x "
+                             f"{steps_taken / args.steps:.4g} steps per launch (device counter); "
+                             "peak = measured FFMA throughput of this GPU (pp_measure_fp32_peak)"},
+        "hits_per_step": n_hits_total / args.steps,
+        "photon_steps_per_step": steps_taken / args.steps,
+        "hit_write_gbs": n_hits_total * 80 / kernel_s / 1e9,
+        "cpu_baseline": base,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+        "wall_s_timed_region": wall,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

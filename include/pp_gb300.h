@@ -1,0 +1,303 @@
+/*
+ * pp_gb300.h -- C ABI of the GB300 (sm_103a) photon-transport library.
+ *
+ * This is the drop-in seam for PhotonPropagation.jl's photon-transport hot path.
+ * Julia reaches it through `ccall`; Python through ctypes.  Every function
+ * returns an int status (pp_status); a message for the last failure on the
+ * calling thread is available from pp_last_error().
+ *
+ * Reference interfaces replaced (PhotonPropagation.jl v0.9.3, paths inside
+ * that project):
+ *   run_photon_prop_no_local_cache!   src/photon_prop_cuda.jl:889-959
+ *   cuda_propagate_photons!           src/photon_prop_cuda.jl:429-549
+ *   make_hit_buffers                  src/photon_prop_cuda.jl:878-886
+ *   PhotonPropOOMException            src/photon_prop_cuda.jl:40, :937-939
+ *   PhotonPropSetup (device tables)   src/photon_propagation_setup.jl:18-25
+ *   make_cuda_spectral_dist           src/spectrum.jl:75-83
+ *
+ * Conventions
+ *   - 0 = success; 1 = hit buffer overflow (the Julia shim throws
+ *     PhotonPropOOMException, as src/photon_prop_cuda.jl:937-939 does);
+ *     negative = invalid argument / CUDA error / bounded device wait gave up.
+ *   - A context owns one device, one internal stream and its device tables.
+ *     Calls on one context are not re-entrant; separate contexts may be used
+ *     from separate threads.
+ *   - pp_propagate is synchronous with respect to the caller (like the
+ *     reference's CUDA.@sync launch, src/photon_prop_cuda.jl:933).  pp_launch
+ *     and pp_launch_graph are asynchronous on the caller's stream.
+ *   - No function ever falls back to a CPU implementation: without a usable
+ *     CUDA device they return PP_ERR_NO_DEVICE.
+ */
+#ifndef PP_GB300_H
+#define PP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define PP_API __declspec(dllexport)
+#else
+#define PP_API __attribute__((visibility("default")))
+#endif
+
+#define PP_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define PP_OK 0
+#define PP_ERR_OVERFLOW 1    /* hit buffer full: PhotonPropOOMException      */
+#define PP_ERR_INVALID (-1)  /* bad argument                                 */
+#define PP_ERR_CUDA (-2)     /* CUDA runtime error (message in last_error)    */
+#define PP_ERR_TIMEOUT (-3)  /* a bounded device-side wait gave up            */
+#define PP_ERR_NOT_READY (-4)/* medium / spectrum / targets / sources missing */
+#define PP_ERR_NO_DEVICE (-5)/* no CUDA device                                */
+
+/* ---- device-side error flag bits (pp_counters.err_flags) ---------------- */
+#define PP_FLAG_OVERFLOW 1u  /* a hit did not fit into the buffer            */
+#define PP_FLAG_TIMEOUT 2u   /* a TMA staging wait hit its iteration limit    */
+
+/* ---- emitter kinds (src/lightyield.jl:437-873, init functions
+ *      src/photon_prop_cuda.jl:158-276) ----------------------------------- */
+#define PP_SRC_POINTLIKE_ISOTROPIC 0        /* lightyield.jl:549, prop:158  */
+#define PP_SRC_EXTENDED_CHERENKOV 1         /* lightyield.jl:616, prop:211  */
+#define PP_SRC_EXTENDED_CHERENKOV_NOSMEAR 2 /* lightyield.jl:670, prop:225  */
+#define PP_SRC_POINTLIKE_CHERENKOV 3        /* prop:254                     */
+#define PP_SRC_CHERENKOV_TRACK 4            /* prop:265                     */
+#define PP_SRC_POINTLIKE_TIME_RANGE 5       /* lightyield.jl:592, prop:165  */
+#define PP_SRC_COLLIMATED_ISOTROPIC 6       /* lightyield.jl:570, prop:186  */
+#define PP_SRC_PENCIL 7                     /* lightyield.jl:527, prop:197  */
+#define PP_SRC_AXICONE 8                    /* lightyield.jl:503, prop:173  */
+#define PP_SRC_KIND_COUNT 9
+
+/* One photon source (96 bytes).  Fields not used by a kind are ignored.
+ * The source emits photons first_photon .. first_photon + n - 1 (n after
+ * scaling); photon i always draws the same random numbers, so a source can be
+ * split into photon ranges (shards, replays) with identical results. */
+typedef struct pp_source {
+  int32_t kind;           /* PP_SRC_*                                         */
+  int32_t reserved0;
+  int64_t photons;        /* PhotonSource.photons (Int64)                     */
+  float position[3];      /* m                                                */
+  float time;             /* ns; time_range[1] for POINTLIKE_TIME_RANGE       */
+  float direction[3];     /* unit axis (Cherenkov, pencil, axicone)           */
+  float time_end;         /* ns; time_range[2] for POINTLIKE_TIME_RANGE       */
+  float long_a;           /* LongitudinalParameterisation.a                   */
+  float long_b;           /* LongitudinalParameterisation.b                   */
+  float long_lrad;        /* LongitudinalParameterisation.lrad (m)            */
+  float length;           /* CherenkovTrackEmitter.length (m)                 */
+  float angle;            /* AxiconeEmitter.angle (rad)                       */
+  float beam_divergence;  /* Axicone / Pencil beam_divergence (rad)           */
+  float cut_angle_cos;    /* CollimatedIsotropicEmitter.cut_angle_cos         */
+  float reserved1;
+  int64_t first_photon;   /* index of the first photon (0 for a whole source) */
+  int64_t reserved2;
+} pp_source;
+
+/* Spherical{Float32} target (NeutrinoTelescopeBase): 16 bytes. */
+typedef struct pp_sphere {
+  float position[3];
+  float radius;
+} pp_sphere;
+
+/* Medium as tables on a uniform wavelength grid, plus the MixedHGES phase
+ * function (CascadiaMediumProperties, src/water_properties.jl:43-100;
+ * SimpleMediumProperties, src/simple_medium.jl:1-15).  The Julia shim fills
+ * the tables with the reference's own scattering_length / group_velocity /
+ * absorption_length / phase_refractive_index. */
+typedef struct pp_medium {
+  float wl_min;                       /* nm of knot 0                        */
+  float wl_step;                      /* nm between knots (> 0)              */
+  int32_t n_knots;                    /* >= 2                                */
+  int32_t reserved0;
+  const float* scattering_length;     /* m    [n_knots]                      */
+  const float* group_velocity;        /* m/ns [n_knots]                      */
+  const float* absorption_length;     /* m    [n_knots]                      */
+  const float* phase_refractive_index;/*      [n_knots]                      */
+  float hg_g;                         /* Henyey-Greenstein mean cosine       */
+  float es_b;                         /* Einstein-Smoluchowski b             */
+  float hg_weight;                    /* P(HG) in the mixture; 1 = pure HG   */
+  float reserved1;
+} pp_medium;
+
+/* Launch tuning (chosen by pp_autotune or set by the caller). */
+typedef struct pp_tuning {
+  int32_t block_threads;      /* CTA size, multiple of 32, 64..1024          */
+  int32_t photons_per_thread; /* photons each lane takes per queued chunk    */
+  int32_t ctas_per_sm;        /* 0 = occupancy maximum                       */
+  int32_t precise_math;       /* 1 = IEEE libm functions (replay checks)     */
+  float cell_size;            /* target-grid cell edge (m); 0 = automatic    */
+  int32_t grid_in_global;     /* 1 = read the grid from global memory        */
+  int32_t reserved[2];
+} pp_tuning;
+
+/* One hit as written by the kernel into device memory: 80 bytes, 16-byte
+ * aligned, stored with vectorised 16-byte stores.  Fields follow PhotonHit
+ * (src/photon_prop_cuda.jl:407-416) plus the absorption weight that the
+ * reference computes on the host (src/processing.jl:32-44). */
+typedef struct pp_hit_record {
+  float position[3];
+  float wavelength;
+  float direction[3];
+  float dist_travelled;
+  float initial_direction[3];
+  float abs_weight;           /* exp(-dist_travelled / absorption_length)     */
+  double time;                /* ns (FP64 accumulator)                         */
+  int64_t photon_index;       /* index of the photon within its source         */
+  int32_t module_index;       /* 1-based index into the target list            */
+  int32_t n_steps;            /* step (1-based) at which the photon hit        */
+  int32_t source_index;       /* 0-based index into the source list            */
+  int32_t reserved;
+} pp_hit_record;
+
+/* Device-side counters of one launch (zeroed by pp_launch / pp_launch_graph). */
+typedef struct pp_counters {
+  uint64_t n_hits;        /* hit slots claimed (> capacity on overflow)      */
+  uint64_t n_ph_sim;      /* photons fully simulated                          */
+  uint64_t photon_steps;  /* scattering steps taken, all photons              */
+  uint64_t work_next;     /* head of the device work queue                    */
+  uint32_t err_flags;     /* PP_FLAG_*                                        */
+  uint32_t reserved[3];
+} pp_counters;
+
+/* Hit table as columns (structure of arrays), host or device memory, each
+ * column caller-allocated with room for `capacity` rows.  Vector columns are
+ * row-major [n][3].  NULL columns are skipped. */
+typedef struct pp_hits {
+  float* position;
+  float* direction;
+  float* initial_direction;
+  float* wavelength;
+  double* time;
+  float* dist_travelled;
+  float* abs_weight;
+  int32_t* module_index;
+  int32_t* n_steps;
+  int32_t* source_index;
+  int64_t* photon_index;
+} pp_hits;
+
+typedef struct pp_ctx pp_ctx;
+
+/* ---- library ------------------------------------------------------------ */
+
+/* ABI version (PP_ABI_VERSION).  No reference counterpart. */
+PP_API int pp_version(void);
+
+/* Copy the calling thread's last error message into buf (always
+ * NUL-terminated); returns the full message length. */
+PP_API int pp_last_error(char* buf, int32_t len);
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Create a context on `device`.  Replaces the implicit CUDA.jl device state
+ * used by run_photon_prop_no_local_cache! (src/photon_prop_cuda.jl:889-912). */
+PP_API int pp_create(pp_ctx** out, int32_t device);
+PP_API int pp_destroy(pp_ctx* ctx);
+
+/* Medium tables (the per-wavelength evaluations the kernel performs with
+ * scattering_length / group_velocity at src/photon_prop_cuda.jl:480-482 and
+ * the host absorption weight at src/processing.jl:38-39). */
+PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* medium);
+
+/* Tabulated inverse CDF of the wavelength spectrum, n knots at u=i/(n-1)
+ * (make_cuda_spectral_dist, src/spectrum.jl:75-83).  Sampled like the
+ * reference's 1-D linear-filtered texture with normalised coordinates. */
+PP_API int pp_set_spectrum(pp_ctx* ctx, const float* inv_cdf_knots, int32_t n);
+
+/* Monochromatic spectrum (Monochromatic, src/spectrum.jl:66-72). */
+PP_API int pp_set_monochromatic(pp_ctx* ctx, float wavelength_nm);
+
+/* Quantile table of cos(theta) of the Cherenkov track direction about the
+ * emitter axis, n knots at u=i/(n-1) (sample_cherenkov_track_direction,
+ * called at src/photon_prop_cuda.jl:89).  Needed by Cherenkov emitters. */
+PP_API int pp_set_track_smear(pp_ctx* ctx, const float* cos_theta_quantiles, int32_t n);
+
+/* Upload spherical targets and build the uniform culling grid on the device.
+ * cell_size <= 0 picks a size automatically.  Replaces CuVector(targets)
+ * (src/photon_prop_cuda.jl:910-912). */
+PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* targets, int32_t n, float cell_size);
+
+/* Upload the source list and build the device work queue.  Photon count of
+ * source i is floor(Float32(photons) * photon_scaling), computed in FP32 as the
+ * reference does (src/photon_prop_cuda.jl:456). */
+PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* sources, int32_t n, float photon_scaling);
+
+PP_API int pp_set_tuning(pp_ctx* ctx, const pp_tuning* tuning);
+PP_API int pp_get_tuning(const pp_ctx* ctx, pp_tuning* tuning);
+
+/* Total photons of the uploaded sources after scaling. */
+PP_API int pp_total_photons(const pp_ctx* ctx, int64_t* total);
+
+/* ---- propagation ---------------------------------------------------------- */
+
+/* Asynchronous launch on `stream` (cudaStream_t; NULL = legacy default
+ * stream): zeroes *d_counters, runs the persistent propagation kernel over
+ * every uploaded source, writes hits into d_hits (device memory, capacity
+ * records).  The device-resident form of cuda_propagate_photons! launched
+ * once per source (src/photon_prop_cuda.jl:927-943): here one launch covers
+ * all sources through a device work queue. */
+PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
+                     int64_t capacity, pp_counters* d_counters, void* stream);
+
+/* Same work as pp_launch, replayed from a CUDA graph (memset + kernel)
+ * captured on first use for these arguments. */
+PP_API int pp_launch_graph(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
+                           int64_t capacity, pp_counters* d_counters, void* stream);
+
+/* Synchronous drop-in for run_photon_prop_no_local_cache!
+ * (src/photon_prop_cuda.jl:889-959): uploads `sources`, propagates, and
+ * copies only the n_hits rows (not the whole buffer) into `out` (host or
+ * device columns with room for `capacity` rows; out = NULL copies nothing,
+ * see pp_fetch_hits).  Returns PP_ERR_OVERFLOW when more than `capacity` hits
+ * occurred (*n_hits then holds the number of hits).  The device hit buffer is
+ * owned by the context and holds min(capacity, photons) records (a photon hits
+ * at most once). */
+PP_API int pp_propagate(pp_ctx* ctx, const pp_source* sources, int32_t n_src, int64_t seed,
+                        int32_t n_steps, float photon_scaling, const pp_hits* out,
+                        int64_t capacity, int64_t* n_hits, int64_t* n_ph_sim);
+
+/* Copy the first n hits of the last pp_propagate on this context into `out`
+ * (host or device columns with room for n rows).  With pp_propagate(out=NULL)
+ * this lets a caller size its output after the hit count is known, copying
+ * only n_hits rows (the reference copies the whole buffer,
+ * src/photon_prop_cuda.jl:950-954). */
+PP_API int pp_fetch_hits(pp_ctx* ctx, const pp_hits* out, int64_t n);
+
+/* Free and total memory of `device` in bytes (CUDA.totalmem as used by
+ * make_hit_buffers, src/photon_prop_cuda.jl:878-880). */
+PP_API int pp_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
+
+/* Scatter n device hit records into device columns (structure of arrays). */
+PP_API int pp_hits_to_columns(const pp_hit_record* d_records, int64_t n, const pp_hits* d_out,
+                              void* stream);
+
+/* Time candidate tunings on a sample of the uploaded sources and keep the
+ * fastest (block size, photons per thread, grid cell size).  No reference
+ * counterpart (the reference uses CUDA.launch_configuration,
+ * src/photon_prop_cuda.jl:914-921). */
+PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sample_photons,
+                       pp_tuning* best, double* best_photons_per_s);
+
+/* ---- diagnostics (no reference counterpart) -------------------------------- */
+
+/* Philox4x32-10 on the device: out[4*i..4*i+3] = philox(ctr[i], key), n rows.
+ * ctr and out are host arrays. */
+PP_API int pp_debug_philox(const uint32_t* ctr, int32_t n, uint32_t key0, uint32_t key1,
+                           uint32_t* out);
+
+/* Measured FP32 FFMA throughput of `device` (TFLOP/s), the denominator of
+ * the propagation kernel's roofline. */
+PP_API int pp_measure_fp32_peak(int32_t device, double* tflops);
+
+/* Grid statistics of the last pp_set_targets (cells per axis, items). */
+PP_API int pp_grid_info(const pp_ctx* ctx, int32_t dims[3], float cell[3], float origin[3],
+                        int64_t* n_items, int64_t* blob_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PP_GB300_H */

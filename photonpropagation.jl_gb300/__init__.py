@@ -1,0 +1,26 @@
+"""GB300-native photon transport behind PhotonPropagation.jl's API.
+
+Host-side mirror of the reference's Julia interface for the photon-transport
+hot path: ``PhotonPropSetup(sources, targets, medium, spectrum, seed)`` and
+``propagate_photons(setup)``.  The propagation itself runs in the sm_103a CUDA
+library ``_lib/libpp_gb300.so`` (C ABI in include/pp_gb300.h); there is no CPU
+path.
+"""
+from . import _lib
+from .context import Context, debug_philox, device_memory, measure_fp32_peak
+from .medium import (C_VAC_M_NS, CascadiaMediumProperties, MediumProperties,
+                     SimpleMediumProperties)
+from .processing import (HitBuffers, HitTable, PhotonPropOOMException, calc_total_weight,
+                         get_context, make_hit_buffers, propagate_photons,
+                         run_photon_prop_no_local_cache)
+from .propsetup import PhotonPropSetup
+from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropicEmitter,
+                      ExtendedCherenkovEmitter, ExtendedCherenkovEmitterNoSmear,
+                      LongitudinalParameterisation, PencilEmitter, PointlikeCherenkovEmitter,
+                      PointlikeIsotropicEmitter, PointlikeTimeRangeEmitter, source_photons)
+from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
+                       make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
+from .targets import HomogeneousDetector, Spherical
+from . import workloads
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,903 @@
+// pp_abi.cu -- the C ABI (include/pp_gb300.h): contexts, device tables, the
+// synchronous drop-in propagate call, asynchronous and graph-replayed
+// launches, and the launch autotuner.
+//
+// Host-side counterpart of run_photon_prop_no_local_cache!
+// (PhotonPropagation.jl v0.9.3, src/photon_prop_cuda.jl:889-959).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pp_internal.h"
+
+using pp::GridDev;
+using pp::LaunchArgs;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  return set_error(PP_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define PP_CUDA(call, what)                  \
+  do {                                       \
+    cudaError_t e_ = (call);                 \
+    if (e_ != cudaSuccess) return cuda_error(e_, what); \
+  } while (0)
+
+// Makes ctx->device current for the scope of one ABI call.
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceScope() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+bool is_device_pointer(const void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+long long source_photons(long long photons, float scaling) {
+  // Int64 * Float32 promotes to Float32 (src/photon_prop_cuda.jl:456).
+  const float x = (float)photons * scaling;
+  if (!(x > 0.0f)) return 0;
+  return (long long)floorf(x);
+}
+
+bool kind_uses_track(int kind) {
+  return kind == PP_SRC_EXTENDED_CHERENKOV || kind == PP_SRC_POINTLIKE_CHERENKOV ||
+         kind == PP_SRC_CHERENKOV_TRACK;
+}
+
+}  // namespace
+
+struct GraphKey {
+  long long seed = 0;
+  int n_steps = 0;
+  const void* hits = nullptr;
+  long long capacity = 0;
+  const void* counters = nullptr;
+  cudaStream_t stream = nullptr;
+  unsigned long long version = 0;
+  bool operator==(const GraphKey& o) const {
+    return seed == o.seed && n_steps == o.n_steps && hits == o.hits && capacity == o.capacity &&
+           counters == o.counters && stream == o.stream && version == o.version;
+  }
+};
+
+struct pp_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  unsigned long long version = 1;
+
+  // medium
+  float4* d_medium = nullptr;
+  int n_medium = 0;
+  float med_wl_min = 0.0f, med_inv_step = 0.0f;
+  pp::PhaseDev phase{};
+  bool has_medium = false;
+
+  // spectrum
+  float* d_spectrum = nullptr;
+  int n_spectrum = 0;
+  float mono = 0.0f;
+  bool has_spectrum = false;
+
+  // Cherenkov track smear quantiles
+  float* d_track = nullptr;
+  int n_track = 0;
+
+  // targets and grid
+  std::vector<pp_sphere> h_targets;
+  pp_sphere* d_targets = nullptr;
+  unsigned char* d_blob = nullptr;
+  GridDev grid{};
+  long long n_items = 0;
+  bool has_targets = false;
+
+  // sources and work queue
+  std::vector<pp_source> h_sources;
+  float scaling = 1.0f;
+  pp_source* d_sources = nullptr;
+  unsigned long long* d_prefix = nullptr;
+  long long* d_src_photons = nullptr;
+  int n_src = 0;
+  int n_src_alloc = 0;
+  unsigned long long total_chunks = 0;
+  long long total_photons = 0;
+  bool has_sources = false;
+  bool needs_track = false;
+
+  pp_tuning tuning{256, 8, 0, 0, 0.0f, 0, {0, 0}};
+
+  // scratch of pp_propagate
+  pp_hit_record* d_hits = nullptr;
+  long long d_hits_cap = 0;
+  pp_counters* d_ctr = nullptr;
+  pp_hit_record* h_stage = nullptr;
+  long long h_stage_cap = 0;
+
+  // cached CUDA graph of pp_launch_graph
+  cudaGraphExec_t gexec = nullptr;
+  GraphKey gkey{};
+
+  long long last_hits = 0;  // hits held in d_hits from the last pp_propagate
+};
+
+namespace {
+
+int build_queue(pp_ctx* ctx) {
+  const int n = (int)ctx->h_sources.size();
+  const long long chunk = 32LL * ctx->tuning.photons_per_thread;
+  std::vector<unsigned long long> prefix(n + 1, 0);
+  std::vector<long long> nph(std::max(n, 1), 0);
+  long long total = 0;
+  for (int i = 0; i < n; ++i) {
+    nph[i] = source_photons(ctx->h_sources[i].photons, ctx->scaling);
+    total += nph[i];
+    prefix[i + 1] = prefix[i] + (unsigned long long)((nph[i] + chunk - 1) / chunk);
+  }
+  if (n > ctx->n_src_alloc) {
+    cudaFree(ctx->d_sources);
+    cudaFree(ctx->d_prefix);
+    cudaFree(ctx->d_src_photons);
+    ctx->d_sources = nullptr;
+    ctx->d_prefix = nullptr;
+    ctx->d_src_photons = nullptr;
+    ctx->n_src_alloc = 0;
+    PP_CUDA(cudaMalloc(&ctx->d_sources, sizeof(pp_source) * n), "cudaMalloc(sources)");
+    PP_CUDA(cudaMalloc(&ctx->d_prefix, sizeof(unsigned long long) * (n + 1)), "cudaMalloc(prefix)");
+    PP_CUDA(cudaMalloc(&ctx->d_src_photons, sizeof(long long) * n), "cudaMalloc(photons)");
+    ctx->n_src_alloc = n;
+  }
+  if (n > 0) {
+    PP_CUDA(cudaMemcpyAsync(ctx->d_sources, ctx->h_sources.data(), sizeof(pp_source) * n,
+                            cudaMemcpyHostToDevice, ctx->stream), "upload sources");
+    PP_CUDA(cudaMemcpyAsync(ctx->d_prefix, prefix.data(), sizeof(unsigned long long) * (n + 1),
+                            cudaMemcpyHostToDevice, ctx->stream), "upload prefix");
+    PP_CUDA(cudaMemcpyAsync(ctx->d_src_photons, nph.data(), sizeof(long long) * n,
+                            cudaMemcpyHostToDevice, ctx->stream), "upload photon counts");
+    PP_CUDA(cudaStreamSynchronize(ctx->stream), "upload sources");
+  }
+  ctx->n_src = n;
+  ctx->total_chunks = prefix[n];
+  ctx->total_photons = total;
+  ctx->version++;
+  return PP_OK;
+}
+
+int rebuild_grid(pp_ctx* ctx, float cell_size) {
+  cudaFree(ctx->d_blob);
+  ctx->d_blob = nullptr;
+  std::string err;
+  GridDev g{};
+  unsigned char* blob = nullptr;
+  long long n_items = 0;
+  const int n = (int)ctx->h_targets.size();
+  if (pp::build_grid(ctx->d_targets, n, cell_size, ctx->stream, &g, &blob, &n_items, &err) != 0)
+    return set_error(PP_ERR_INVALID, "pp_set_targets: %s", err.c_str());
+  ctx->grid = g;
+  ctx->d_blob = blob;
+  ctx->n_items = n_items;
+  ctx->version++;
+  return PP_OK;
+}
+
+int check_ready(const pp_ctx* ctx) {
+  if (!ctx->has_medium) return set_error(PP_ERR_NOT_READY, "medium not set (pp_set_medium)");
+  if (!ctx->has_spectrum)
+    return set_error(PP_ERR_NOT_READY, "spectrum not set (pp_set_spectrum / pp_set_monochromatic)");
+  if (!ctx->has_targets) return set_error(PP_ERR_NOT_READY, "targets not set (pp_set_targets)");
+  if (!ctx->has_sources) return set_error(PP_ERR_NOT_READY, "sources not set (pp_set_sources)");
+  if (ctx->needs_track && ctx->n_track < 2)
+    return set_error(PP_ERR_NOT_READY,
+                     "Cherenkov emitters need the track-direction table (pp_set_track_smear)");
+  return PP_OK;
+}
+
+bool use_smem_grid(const pp_ctx* ctx) {
+  return !ctx->tuning.grid_in_global && ctx->grid.blob_bytes <= pp::max_smem_blob_bytes();
+}
+
+LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_record* hits,
+                     long long capacity, pp_counters* ctr) {
+  LaunchArgs a{};
+  a.sources = ctx->d_sources;
+  a.chunk_prefix = ctx->d_prefix;
+  a.src_photons = ctx->d_src_photons;
+  a.total_chunks = ctx->total_chunks;
+  a.n_src = ctx->n_src;
+  a.chunk_photons = 32 * ctx->tuning.photons_per_thread;
+  a.blob = ctx->d_blob;
+  a.grid = ctx->grid;
+  a.medium = ctx->d_medium;
+  a.n_medium = ctx->n_medium;
+  a.med_wl_min = ctx->med_wl_min;
+  a.med_inv_step = ctx->med_inv_step;
+  a.phase = ctx->phase;
+  a.spectrum = ctx->n_spectrum > 0 ? ctx->d_spectrum : nullptr;
+  a.n_spectrum = ctx->n_spectrum;
+  a.mono_wavelength = ctx->mono;
+  a.track = ctx->d_track;
+  a.n_track = ctx->n_track;
+  a.key0 = (uint32_t)((unsigned long long)seed & 0xffffffffu);
+  a.key1 = (uint32_t)((unsigned long long)seed >> 32);
+  a.n_steps = n_steps;
+  a.hits = hits;
+  a.capacity = capacity > 0 ? (unsigned long long)capacity : 0ull;
+  a.counters = ctr;
+  a.wait_limit_ns = 2000000000ull;
+  return a;
+}
+
+int enqueue(pp_ctx* ctx, long long seed, int n_steps, pp_hit_record* d_hits, long long capacity,
+            pp_counters* d_ctr, cudaStream_t stream) {
+  PP_CUDA(cudaMemsetAsync(d_ctr, 0, sizeof(pp_counters), stream), "zero counters");
+  if (ctx->total_chunks == 0) return PP_OK;
+  const LaunchArgs a = make_args(ctx, seed, n_steps, d_hits, capacity, d_ctr);
+  int grid = 0;
+  cudaError_t e = pp::launch_propagate(a, ctx->tuning.block_threads, ctx->tuning.ctas_per_sm,
+                                       ctx->tuning.precise_math != 0, use_smem_grid(ctx),
+                                       ctx->num_sms, stream, &grid);
+  if (e != cudaSuccess) return cuda_error(e, "launch propagate kernel");
+  return PP_OK;
+}
+
+int validate_launch(pp_ctx* ctx, int n_steps, const void* d_hits, long long capacity,
+                    const void* d_ctr) {
+  if (!ctx) return set_error(PP_ERR_INVALID, "null context");
+  if (n_steps < 1) return set_error(PP_ERR_INVALID, "n_steps must be >= 1 (got %d)", n_steps);
+  if (!d_ctr) return set_error(PP_ERR_INVALID, "null counters pointer");
+  if (capacity < 0) return set_error(PP_ERR_INVALID, "negative capacity");
+  if (capacity > 0 && !d_hits) return set_error(PP_ERR_INVALID, "null hit buffer");
+  if (((uintptr_t)d_hits & 15u) != 0) return set_error(PP_ERR_INVALID, "hit buffer not 16-byte aligned");
+  return check_ready(ctx);
+}
+
+int fetch_hits(pp_ctx* ctx, const pp_hits* out, long long n);
+
+}  // namespace
+
+extern "C" {
+
+PP_API int pp_version(void) { return PP_ABI_VERSION; }
+
+PP_API int pp_last_error(char* buf, int32_t len) {
+  const int n = (int)g_last_error.size();
+  if (buf && len > 0) {
+    const int m = std::min(n, len - 1);
+    memcpy(buf, g_last_error.data(), m);
+    buf[m] = '\0';
+  }
+  return n;
+}
+
+PP_API int pp_create(pp_ctx** out, int32_t device) {
+  if (!out) return set_error(PP_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return set_error(PP_ERR_NO_DEVICE, "no CUDA device available (%s)",
+                     e != cudaSuccess ? cudaGetErrorString(e) : "device count is 0");
+  }
+  if (device < 0 || device >= count)
+    return set_error(PP_ERR_INVALID, "device %d out of range [0, %d)", device, count);
+  DeviceScope ds(device);
+  pp_ctx* ctx = new pp_ctx();
+  ctx->device = device;
+  e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctr, sizeof(pp_counters));
+  if (e != cudaSuccess) {
+    int rc = cuda_error(e, "pp_create");
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return rc;
+  }
+  *out = ctx;
+  return PP_OK;
+}
+
+PP_API int pp_destroy(pp_ctx* ctx) {
+  if (!ctx) return PP_OK;
+  DeviceScope ds(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  cudaFree(ctx->d_medium);
+  cudaFree(ctx->d_spectrum);
+  cudaFree(ctx->d_track);
+  cudaFree(ctx->d_targets);
+  cudaFree(ctx->d_blob);
+  cudaFree(ctx->d_sources);
+  cudaFree(ctx->d_prefix);
+  cudaFree(ctx->d_src_photons);
+  cudaFree(ctx->d_hits);
+  cudaFree(ctx->d_ctr);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return PP_OK;
+}
+
+PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
+  if (!ctx || !m) return set_error(PP_ERR_INVALID, "null argument");
+  if (m->n_knots < 2 || !(m->wl_step > 0.0f) || !std::isfinite(m->wl_min))
+    return set_error(PP_ERR_INVALID, "medium grid needs n_knots >= 2 and wl_step > 0");
+  if (!m->scattering_length || !m->group_velocity || !m->absorption_length ||
+      !m->phase_refractive_index)
+    return set_error(PP_ERR_INVALID, "medium table pointer is null");
+  if (!(m->hg_weight >= 0.0f && m->hg_weight <= 1.0f))
+    return set_error(PP_ERR_INVALID, "hg_weight must be in [0, 1]");
+  if (m->hg_weight > 0.0f && !(fabsf(m->hg_g) >= 1e-3f && fabsf(m->hg_g) < 1.0f))
+    return set_error(PP_ERR_INVALID, "hg_g must satisfy 1e-3 <= |g| < 1");
+  if (m->hg_weight < 1.0f && !(m->es_b > 0.0f))
+    return set_error(PP_ERR_INVALID, "es_b must be > 0 when the ES component is used");
+  std::vector<float4> t(m->n_knots);
+  for (int i = 0; i < m->n_knots; ++i) {
+    const float s = m->scattering_length[i], v = m->group_velocity[i];
+    const float ab = m->absorption_length[i], n = m->phase_refractive_index[i];
+    if (!(s > 0.0f) || !(v > 0.0f) || !(ab > 0.0f) || !(n > 0.0f) || !std::isfinite(s) ||
+        !std::isfinite(v) || !std::isfinite(n))
+      return set_error(PP_ERR_INVALID, "medium table entry %d is not positive and finite", i);
+    t[i] = make_float4(s, v, ab, n);
+  }
+  DeviceScope ds(ctx->device);
+  cudaFree(ctx->d_medium);
+  ctx->d_medium = nullptr;
+  PP_CUDA(cudaMalloc(&ctx->d_medium, sizeof(float4) * t.size()), "cudaMalloc(medium)");
+  PP_CUDA(cudaMemcpy(ctx->d_medium, t.data(), sizeof(float4) * t.size(), cudaMemcpyHostToDevice),
+          "upload medium");
+  ctx->n_medium = m->n_knots;
+  ctx->med_wl_min = m->wl_min;
+  ctx->med_inv_step = 1.0f / m->wl_step;
+  pp::PhaseDev& p = ctx->phase;
+  p.hg_weight = m->hg_weight;
+  p.hg_g = m->hg_g;
+  p.hg_1mg2 = 1.0f - m->hg_g * m->hg_g;
+  p.hg_1pg2 = 1.0f + m->hg_g * m->hg_g;
+  p.hg_inv2g = m->hg_weight > 0.0f ? 1.0f / (2.0f * m->hg_g) : 0.0f;
+  const float b = m->es_b > 0.0f ? m->es_b : 1.0f;
+  p.es_k1 = (b + 3.0f) / b;
+  p.es_k2 = 1.0f / (b * b * b);
+  ctx->has_medium = true;
+  ctx->version++;
+  return PP_OK;
+}
+
+PP_API int pp_set_spectrum(pp_ctx* ctx, const float* knots, int32_t n) {
+  if (!ctx || !knots || n < 1) return set_error(PP_ERR_INVALID, "spectrum needs n >= 1 knots");
+  for (int i = 0; i < n; ++i)
+    if (!(knots[i] > 0.0f) || !std::isfinite(knots[i]))
+      return set_error(PP_ERR_INVALID, "spectrum knot %d is not a positive wavelength", i);
+  DeviceScope ds(ctx->device);
+  cudaFree(ctx->d_spectrum);
+  ctx->d_spectrum = nullptr;
+  PP_CUDA(cudaMalloc(&ctx->d_spectrum, sizeof(float) * n), "cudaMalloc(spectrum)");
+  PP_CUDA(cudaMemcpy(ctx->d_spectrum, knots, sizeof(float) * n, cudaMemcpyHostToDevice),
+          "upload spectrum");
+  ctx->n_spectrum = n;
+  ctx->has_spectrum = true;
+  ctx->version++;
+  return PP_OK;
+}
+
+PP_API int pp_set_monochromatic(pp_ctx* ctx, float wavelength) {
+  if (!ctx || !(wavelength > 0.0f) || !std::isfinite(wavelength))
+    return set_error(PP_ERR_INVALID, "monochromatic wavelength must be positive");
+  DeviceScope ds(ctx->device);
+  cudaFree(ctx->d_spectrum);
+  ctx->d_spectrum = nullptr;
+  ctx->n_spectrum = 0;
+  ctx->mono = wavelength;
+  ctx->has_spectrum = true;
+  ctx->version++;
+  return PP_OK;
+}
+
+PP_API int pp_set_track_smear(pp_ctx* ctx, const float* q, int32_t n) {
+  if (!ctx || !q || n < 2) return set_error(PP_ERR_INVALID, "track table needs n >= 2 knots");
+  for (int i = 0; i < n; ++i)
+    if (!(q[i] >= -1.0f && q[i] <= 1.0f))
+      return set_error(PP_ERR_INVALID, "track quantile %d outside [-1, 1]", i);
+  DeviceScope ds(ctx->device);
+  cudaFree(ctx->d_track);
+  ctx->d_track = nullptr;
+  PP_CUDA(cudaMalloc(&ctx->d_track, sizeof(float) * n), "cudaMalloc(track)");
+  PP_CUDA(cudaMemcpy(ctx->d_track, q, sizeof(float) * n, cudaMemcpyHostToDevice), "upload track");
+  ctx->n_track = n;
+  ctx->version++;
+  return PP_OK;
+}
+
+PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell_size) {
+  if (!ctx || n < 0 || (n > 0 && !t)) return set_error(PP_ERR_INVALID, "bad target list");
+  if (n > 65535) return set_error(PP_ERR_INVALID, "at most 65535 targets are supported");
+  for (int i = 0; i < n; ++i) {
+    if (!(t[i].radius > 0.0f) || !std::isfinite(t[i].radius) || !std::isfinite(t[i].position[0]) ||
+        !std::isfinite(t[i].position[1]) || !std::isfinite(t[i].position[2]))
+      return set_error(PP_ERR_INVALID, "target %d has a non-finite position or radius <= 0", i);
+  }
+  DeviceScope ds(ctx->device);
+  ctx->h_targets.assign(t, t + n);
+  cudaFree(ctx->d_targets);
+  ctx->d_targets = nullptr;
+  if (n > 0) {
+    PP_CUDA(cudaMalloc(&ctx->d_targets, sizeof(pp_sphere) * n), "cudaMalloc(targets)");
+    PP_CUDA(cudaMemcpy(ctx->d_targets, t, sizeof(pp_sphere) * n, cudaMemcpyHostToDevice),
+            "upload targets");
+  }
+  const float h = cell_size > 0.0f ? cell_size : ctx->tuning.cell_size;
+  int rc = rebuild_grid(ctx, h);
+  if (rc != PP_OK) {
+    ctx->has_targets = false;
+    return rc;
+  }
+  ctx->has_targets = true;
+  return PP_OK;
+}
+
+PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float photon_scaling) {
+  if (!ctx || n < 0 || (n > 0 && !s)) return set_error(PP_ERR_INVALID, "bad source list");
+  if (!(photon_scaling >= 0.0f) || !std::isfinite(photon_scaling))
+    return set_error(PP_ERR_INVALID, "photon_scaling must be finite and >= 0");
+  bool needs_track = false;
+  for (int i = 0; i < n; ++i) {
+    const pp_source& x = s[i];
+    if (x.kind < 0 || x.kind >= PP_SRC_KIND_COUNT)
+      return set_error(PP_ERR_INVALID, "source %d has unknown kind %d", i, x.kind);
+    if (x.photons < 0) return set_error(PP_ERR_INVALID, "source %d has negative photons", i);
+    if (x.kind == PP_SRC_EXTENDED_CHERENKOV || x.kind == PP_SRC_EXTENDED_CHERENKOV_NOSMEAR) {
+      if (!(x.long_a > 0.0f) || !(x.long_b > 0.0f) || !(x.long_lrad >= 0.0f))
+        return set_error(PP_ERR_INVALID, "source %d: longitudinal parameters must be positive", i);
+    }
+    if (kind_uses_track(x.kind)) needs_track = true;
+  }
+  DeviceScope ds(ctx->device);
+  ctx->h_sources.assign(s, s + n);
+  ctx->scaling = photon_scaling;
+  ctx->needs_track = needs_track;
+  int rc = build_queue(ctx);
+  ctx->has_sources = rc == PP_OK;
+  return rc;
+}
+
+PP_API int pp_set_tuning(pp_ctx* ctx, const pp_tuning* t) {
+  if (!ctx || !t) return set_error(PP_ERR_INVALID, "null argument");
+  if (t->block_threads < 64 || t->block_threads > 1024 || (t->block_threads % 32) != 0)
+    return set_error(PP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 1024]");
+  if (t->photons_per_thread < 1 || t->photons_per_thread > 4096)
+    return set_error(PP_ERR_INVALID, "photons_per_thread must be in [1, 4096]");
+  if (t->ctas_per_sm < 0) return set_error(PP_ERR_INVALID, "ctas_per_sm must be >= 0");
+  DeviceScope ds(ctx->device);
+  const bool ppt_changed = t->photons_per_thread != ctx->tuning.photons_per_thread;
+  const bool cell_changed = t->cell_size != ctx->tuning.cell_size;
+  ctx->tuning = *t;
+  ctx->version++;
+  if (ppt_changed && ctx->has_sources) {
+    int rc = build_queue(ctx);
+    if (rc != PP_OK) return rc;
+  }
+  if (cell_changed && ctx->has_targets) {
+    int rc = rebuild_grid(ctx, t->cell_size);
+    if (rc != PP_OK) return rc;
+  }
+  return PP_OK;
+}
+
+PP_API int pp_get_tuning(const pp_ctx* ctx, pp_tuning* t) {
+  if (!ctx || !t) return set_error(PP_ERR_INVALID, "null argument");
+  *t = ctx->tuning;
+  return PP_OK;
+}
+
+PP_API int pp_total_photons(const pp_ctx* ctx, int64_t* total) {
+  if (!ctx || !total) return set_error(PP_ERR_INVALID, "null argument");
+  *total = ctx->total_photons;
+  return PP_OK;
+}
+
+PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
+                     int64_t capacity, pp_counters* d_counters, void* stream) {
+  int rc = validate_launch(ctx, n_steps, d_hits, capacity, d_counters);
+  if (rc != PP_OK) return rc;
+  DeviceScope ds(ctx->device);
+  return enqueue(ctx, seed, n_steps, d_hits, capacity, d_counters, (cudaStream_t)stream);
+}
+
+PP_API int pp_launch_graph(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
+                           int64_t capacity, pp_counters* d_counters, void* stream) {
+  int rc = validate_launch(ctx, n_steps, d_hits, capacity, d_counters);
+  if (rc != PP_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread)
+    return set_error(PP_ERR_INVALID, "pp_launch_graph needs a created (non-default) stream");
+  DeviceScope ds(ctx->device);
+  GraphKey key;
+  key.seed = seed;
+  key.n_steps = n_steps;
+  key.hits = d_hits;
+  key.capacity = capacity;
+  key.counters = d_counters;
+  key.stream = s;
+  key.version = ctx->version;
+  if (!ctx->gexec || !(ctx->gkey == key)) {
+    if (ctx->gexec) {
+      cudaGraphExecDestroy(ctx->gexec);
+      ctx->gexec = nullptr;
+    }
+    PP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int erc = enqueue(ctx, seed, n_steps, d_hits, capacity, d_counters, s);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (erc != PP_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return erc;
+    }
+    if (ce != cudaSuccess) return cuda_error(ce, "end capture");
+    ce = cudaGraphInstantiate(&ctx->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      ctx->gexec = nullptr;
+      return cuda_error(ce, "instantiate graph");
+    }
+    ctx->gkey = key;
+  }
+  PP_CUDA(cudaGraphLaunch(ctx->gexec, s), "graph launch");
+  return PP_OK;
+}
+
+PP_API int pp_hits_to_columns(const pp_hit_record* d_records, int64_t n, const pp_hits* d_out,
+                              void* stream) {
+  if (n < 0 || !d_out || (n > 0 && !d_records)) return set_error(PP_ERR_INVALID, "bad arguments");
+  cudaError_t e = pp::launch_hits_to_columns(d_records, n, *d_out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_error(e, "hits_to_columns");
+  return PP_OK;
+}
+
+PP_API int pp_propagate(pp_ctx* ctx, const pp_source* sources, int32_t n_src, int64_t seed,
+                        int32_t n_steps, float photon_scaling, const pp_hits* out,
+                        int64_t capacity, int64_t* n_hits, int64_t* n_ph_sim) {
+  if (!ctx || !n_hits || !n_ph_sim) return set_error(PP_ERR_INVALID, "null argument");
+  if (capacity < 0) return set_error(PP_ERR_INVALID, "negative capacity");
+  if (n_steps < 1) return set_error(PP_ERR_INVALID, "n_steps must be >= 1");
+  *n_hits = 0;
+  *n_ph_sim = 0;
+  ctx->last_hits = 0;
+  DeviceScope ds(ctx->device);
+  int rc = pp_set_sources(ctx, sources, n_src, photon_scaling);
+  if (rc != PP_OK) return rc;
+  rc = check_ready(ctx);
+  if (rc != PP_OK) return rc;
+  // A photon hits at most once: the device buffer never needs more rows than
+  // there are photons.
+  const long long dev_cap = std::max<long long>(1, std::min<long long>(capacity, ctx->total_photons));
+  if (dev_cap > ctx->d_hits_cap) {
+    cudaFree(ctx->d_hits);
+    ctx->d_hits = nullptr;
+    ctx->d_hits_cap = 0;
+    PP_CUDA(cudaMalloc(&ctx->d_hits, sizeof(pp_hit_record) * dev_cap), "cudaMalloc(hit buffer)");
+    ctx->d_hits_cap = dev_cap;
+  }
+  rc = enqueue(ctx, seed, n_steps, ctx->d_hits, std::min<long long>(capacity, dev_cap), ctx->d_ctr,
+               ctx->stream);
+  if (rc != PP_OK) return rc;
+  pp_counters c{};
+  PP_CUDA(cudaMemcpyAsync(&c, ctx->d_ctr, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream),
+          "read counters");
+  PP_CUDA(cudaStreamSynchronize(ctx->stream), "propagate");
+  *n_hits = (int64_t)c.n_hits;
+  *n_ph_sim = (int64_t)c.n_ph_sim;
+  if (c.err_flags & PP_FLAG_TIMEOUT)
+    return set_error(PP_ERR_TIMEOUT, "a bounded device wait (TMA staging) timed out");
+  if ((c.err_flags & PP_FLAG_OVERFLOW) || (long long)c.n_hits > capacity)
+    return set_error(PP_ERR_OVERFLOW, "hit buffer overflow: %llu hits, capacity %lld",
+                     (unsigned long long)c.n_hits, (long long)capacity);
+  const long long n = (long long)c.n_hits;
+  ctx->last_hits = n;
+  if (n == 0 || !out) return PP_OK;
+  return fetch_hits(ctx, out, n);
+}
+
+PP_API int pp_fetch_hits(pp_ctx* ctx, const pp_hits* out, int64_t n) {
+  if (!ctx || !out || n < 0) return set_error(PP_ERR_INVALID, "bad arguments");
+  if (n > ctx->last_hits)
+    return set_error(PP_ERR_INVALID, "only %lld hits are held", (long long)ctx->last_hits);
+  if (n == 0) return PP_OK;
+  DeviceScope ds(ctx->device);
+  return fetch_hits(ctx, out, n);
+}
+
+PP_API int pp_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return set_error(PP_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0 || device >= count) return set_error(PP_ERR_INVALID, "bad device");
+  DeviceScope ds(device);
+  size_t f = 0, t = 0;
+  PP_CUDA(cudaMemGetInfo(&f, &t), "cudaMemGetInfo");
+  if (free_bytes) *free_bytes = (int64_t)f;
+  if (total_bytes) *total_bytes = (int64_t)t;
+  return PP_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int fetch_hits(pp_ctx* ctx, const pp_hits* out, long long n) {
+  const void* first = out->position ? (const void*)out->position
+                      : out->time   ? (const void*)out->time
+                      : out->module_index ? (const void*)out->module_index
+                                          : (const void*)out->wavelength;
+  if (first && is_device_pointer(first)) {
+    cudaError_t e = pp::launch_hits_to_columns(ctx->d_hits, n, *out, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_error(e, "hits_to_columns");
+    return PP_OK;
+  }
+  if (n > ctx->h_stage_cap) {
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_cap = 0;
+    PP_CUDA(cudaMallocHost(&ctx->h_stage, sizeof(pp_hit_record) * n), "cudaMallocHost(stage)");
+    ctx->h_stage_cap = n;
+  }
+  PP_CUDA(cudaMemcpyAsync(ctx->h_stage, ctx->d_hits, sizeof(pp_hit_record) * n,
+                          cudaMemcpyDeviceToHost, ctx->stream),
+          "copy hits");
+  PP_CUDA(cudaStreamSynchronize(ctx->stream), "copy hits");
+  for (long long i = 0; i < n; ++i) {
+    const pp_hit_record& h = ctx->h_stage[i];
+    for (int a = 0; a < 3; ++a) {
+      if (out->position) out->position[3 * i + a] = h.position[a];
+      if (out->direction) out->direction[3 * i + a] = h.direction[a];
+      if (out->initial_direction) out->initial_direction[3 * i + a] = h.initial_direction[a];
+    }
+    if (out->wavelength) out->wavelength[i] = h.wavelength;
+    if (out->time) out->time[i] = h.time;
+    if (out->dist_travelled) out->dist_travelled[i] = h.dist_travelled;
+    if (out->abs_weight) out->abs_weight[i] = h.abs_weight;
+    if (out->module_index) out->module_index[i] = h.module_index;
+    if (out->n_steps) out->n_steps[i] = h.n_steps;
+    if (out->source_index) out->source_index[i] = h.source_index;
+    if (out->photon_index) out->photon_index[i] = h.photon_index;
+  }
+  return PP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sample_photons,
+                       pp_tuning* best_out, double* best_rate) {
+  if (!ctx) return set_error(PP_ERR_INVALID, "null context");
+  int rc = check_ready(ctx);
+  if (rc != PP_OK) return rc;
+  if (n_steps < 1) return set_error(PP_ERR_INVALID, "n_steps must be >= 1");
+  if (ctx->total_photons <= 0) return set_error(PP_ERR_INVALID, "no photons to tune on");
+  DeviceScope ds(ctx->device);
+  const std::vector<pp_source> orig = ctx->h_sources;
+  const float orig_scaling = ctx->scaling;
+  const pp_tuning orig_tuning = ctx->tuning;
+
+  // Sample: every source scaled by the same factor (at least one photon).
+  const long long want = sample_photons > 0 ? sample_photons : 4000000;
+  const double f = std::min(1.0, (double)want / (double)ctx->total_photons);
+  std::vector<pp_source> sample = orig;
+  for (auto& s : sample) {
+    const long long n = source_photons(s.photons, orig_scaling);
+    s.photons = n > 0 ? std::max<long long>(1, (long long)std::llround(n * f)) : 0;
+  }
+  ctx->h_sources = sample;
+  ctx->scaling = 1.0f;
+
+  pp_hit_record* d_hits = nullptr;
+  pp_counters* d_ctr = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  long long cap = 0;
+  for (const auto& s : sample) cap += s.photons;
+  cap = std::max<long long>(cap, 1);
+  auto finish = [&](int code) {
+    cudaFree(d_hits);
+    cudaFree(d_ctr);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    ctx->h_sources = orig;
+    ctx->scaling = orig_scaling;
+    return code;
+  };
+  if (cudaMalloc(&d_hits, sizeof(pp_hit_record) * cap) != cudaSuccess ||
+      cudaMalloc(&d_ctr, sizeof(pp_counters)) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->tuning = orig_tuning;
+    finish(0);
+    build_queue(ctx);
+    return set_error(PP_ERR_CUDA, "autotune: allocation failed");
+  }
+
+  auto time_config = [&](const pp_tuning& t, double* ms_out) -> int {
+    ctx->tuning = t;
+    int r = build_queue(ctx);
+    if (r != PP_OK) return r;
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, ctx->stream);
+      r = enqueue(ctx, seed, n_steps, d_hits, cap, d_ctr, ctx->stream);
+      if (r != PP_OK) return r;
+      cudaEventRecord(e1, ctx->stream);
+      cudaError_t ce = cudaEventSynchronize(e1);
+      if (ce != cudaSuccess) return cuda_error(ce, "autotune launch");
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) best = std::min(best, ms);
+    }
+    *ms_out = best;
+    return PP_OK;
+  };
+
+  // Stage 1: cell size at the current launch shape.  Stage 2: launch shape at
+  // the best cell size.
+  float auto_h = ctx->grid.cell[0];
+  if (ctx->tuning.cell_size <= 0.0f) {
+    // recover the automatic size
+    auto_h = ctx->grid.cell[0];
+  }
+  pp_tuning best = orig_tuning;
+  double best_ms = 1e300;
+  const float cell_factors[] = {0.5f, 0.75f, 1.0f, 1.5f, 2.0f, 3.0f};
+  float best_h = ctx->grid.cell[0];
+  if (!ctx->h_targets.empty()) {
+    for (float cf : cell_factors) {
+      pp_tuning t = best;
+      t.cell_size = auto_h * cf;
+      if (rebuild_grid(ctx, t.cell_size) != PP_OK) continue;
+      double ms;
+      if (time_config(t, &ms) != PP_OK) continue;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_h = t.cell_size;
+      }
+    }
+    best.cell_size = best_h;
+    if (rebuild_grid(ctx, best_h) != PP_OK) {
+      ctx->tuning = orig_tuning;
+      finish(0);
+      build_queue(ctx);
+      return PP_ERR_INVALID;
+    }
+  }
+  best_ms = 1e300;
+  const int blocks[] = {128, 256, 512};
+  const int ppts[] = {1, 2, 4, 8, 16};
+  for (int b : blocks) {
+    for (int p : ppts) {
+      pp_tuning t = best;
+      t.block_threads = b;
+      t.photons_per_thread = p;
+      double ms;
+      if (time_config(t, &ms) != PP_OK) continue;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best.block_threads = b;
+        best.photons_per_thread = p;
+      }
+    }
+  }
+  finish(0);
+  ctx->tuning = best;
+  rc = build_queue(ctx);
+  if (rc != PP_OK) return rc;
+  if (best_out) *best_out = best;
+  if (best_rate) *best_rate = best_ms < 1e300 ? (double)cap / (best_ms * 1e-3) : 0.0;
+  return best_ms < 1e300 ? PP_OK : set_error(PP_ERR_CUDA, "autotune: no configuration ran");
+}
+
+PP_API int pp_debug_philox(const uint32_t* ctr, int32_t n, uint32_t key0, uint32_t key1,
+                           uint32_t* out) {
+  if (!ctr || !out || n < 0) return set_error(PP_ERR_INVALID, "bad arguments");
+  if (n == 0) return PP_OK;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return set_error(PP_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  uint32_t *dc = nullptr, *dout = nullptr;
+  const size_t bytes = sizeof(uint32_t) * 4 * (size_t)n;
+  cudaError_t e = cudaMalloc(&dc, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&dout, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(dc, ctr, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = pp::launch_debug_philox(dc, n, key0, key1, dout, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(dc);
+  cudaFree(dout);
+  if (e != cudaSuccess) return cuda_error(e, "pp_debug_philox");
+  return PP_OK;
+}
+
+PP_API int pp_measure_fp32_peak(int32_t device, double* tflops) {
+  if (!tflops) return set_error(PP_ERR_INVALID, "null argument");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return set_error(PP_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  DeviceScope ds(device);
+  int sms = 0;
+  PP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attribute");
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  float* sink = nullptr;
+  cudaStream_t s = nullptr;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaMalloc(&sink, sizeof(float) * blocks);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(a, s);
+    e = pp::launch_fp32_peak(sink, blocks, threads, iters, s);
+    cudaEventRecord(b, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaFree(sink);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  if (s) cudaStreamDestroy(s);
+  if (e != cudaSuccess) return cuda_error(e, "pp_measure_fp32_peak");
+  const double flops = (double)blocks * threads * iters * 16.0 * 8.0 * 2.0;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return PP_OK;
+}
+
+PP_API int pp_grid_info(const pp_ctx* ctx, int32_t dims[3], float cell[3], float origin[3],
+                        int64_t* n_items, int64_t* blob_bytes) {
+  if (!ctx) return set_error(PP_ERR_INVALID, "null context");
+  for (int a = 0; a < 3; ++a) {
+    if (dims) dims[a] = ctx->grid.dims[a];
+    if (cell) cell[a] = ctx->grid.cell[a];
+    if (origin) origin[a] = ctx->grid.lo[a];
+  }
+  if (n_items) *n_items = ctx->n_items;
+  if (blob_bytes) *blob_bytes = ctx->grid.blob_bytes;
+  return PP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,348 @@
+// pp_device.cuh -- device-side step functions of the photon-transport kernel.
+//
+// Each function states the PhotonPropagation.jl v0.9.3 function it stands in
+// for (paths inside that project).  Every function comes in two precisions of
+// the transcendental functions: kPrecise = true uses the IEEE-accurate CUDA
+// math library (used by the replay tests), kPrecise = false uses the SFU
+// approximations (lg2/ex2/sin/cos/rcp/sqrt .approx), whose absolute error is
+// below 1e-6 on the argument ranges used here.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pp_internal.h"
+
+namespace ppdev {
+
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u;
+constexpr uint32_t kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u;
+constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
+constexpr uint32_t kExtraCall = 0x80000000u;  // first call of the emitter stream
+constexpr int kGammaMaxTries = 64;
+constexpr float kTwoPi = 6.2831855f;           // Float32(2*pi)
+constexpr float kPi = 3.14159274f;
+constexpr float kCVac = 0.299792458f;          // m/ns
+
+// ---- Philox4x32-10 (Salmon et al., SC'11) --------------------------------
+// Counter = (photon lo, photon hi, call, source), key = seed (lo, hi).
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += kPhiloxW0;
+      k1 += kPhiloxW1;
+    }
+    const unsigned long long p0 = (unsigned long long)kPhiloxM0 * c.x;
+    const unsigned long long p1 = (unsigned long long)kPhiloxM1 * c.z;
+    c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1,
+                   (uint32_t)p0);
+  }
+  return c;
+}
+
+// 24-bit uniform in (0, 1] (exact: integer <= 2^24 times 2^-24).
+__device__ __forceinline__ float u01(uint32_t x) {
+  return __uint2float_rn((x >> 8) + 1u) * 5.9604644775390625e-8f;
+}
+
+// ---- precision-selected primitives -----------------------------------------
+__device__ __forceinline__ float approx_sqrt(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float approx_rcp(float x) {
+  float y;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float approx_lg2(float x) {
+  float y;
+  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float approx_ex2(float x) {
+  float y;
+  asm("ex2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+template <bool P>
+__device__ __forceinline__ float f_log(float x) {
+  if (P) return logf(x);
+  return approx_lg2(x) * 0.693147182f;  // ln(x) = log2(x) * ln(2)
+}
+template <bool P>
+__device__ __forceinline__ float f_sqrt(float x) {
+  return P ? __fsqrt_rn(x) : approx_sqrt(x);
+}
+template <bool P>
+__device__ __forceinline__ float f_rcp(float x) {
+  return P ? __frcp_rn(x) : approx_rcp(x);
+}
+template <bool P>
+__device__ __forceinline__ float f_div(float a, float b) {
+  return P ? __fdiv_rn(a, b) : a * approx_rcp(b);
+}
+// Cube root of a positive number: 2^(log2(x)/3).
+template <bool P>
+__device__ __forceinline__ float f_cbrt_pos(float x) {
+  return P ? cbrtf(x) : approx_ex2(approx_lg2(x) * 0.333333343f);
+}
+template <bool P>
+__device__ __forceinline__ float f_exp(float x) {
+  return P ? expf(x) : approx_ex2(x * 1.44269502f);
+}
+// sin / cos of 2*pi*u for u in (0, 1].  The fast form evaluates the SFU at
+// 2*pi*u - pi, inside [-pi, pi] where its error is smallest, and flips signs.
+template <bool P>
+__device__ __forceinline__ void f_sincos_2pi(float u, float* s, float* c) {
+  if (P) {
+    sincosf(kTwoPi * u, s, c);
+  } else {
+    float ss, cc;
+    __sincosf(fmaf(kTwoPi, u, -kPi), &ss, &cc);
+    *s = -ss;
+    *c = -cc;
+  }
+}
+template <bool P>
+__device__ __forceinline__ void f_sincos(float x, float* s, float* c) {
+  if (P) sincosf(x, s, c); else __sincosf(x, s, c);
+}
+
+// ---- geometry ----------------------------------------------------------------
+// Rotation taking e_z onto the unit vector a, applied to b (rot_from_ez_fast,
+// PhysicsTools; called at src/photon_prop_cuda.jl:92-95, :296).  Written in
+// the Rodrigues form whose only division is well conditioned in each
+// hemisphere of a.
+template <bool P>
+__device__ __forceinline__ float3 rot_from_ez(float3 a, float3 b) {
+  const float s2 = a.x * a.x + a.y * a.y;
+  if (s2 == 0.0f) {
+    const float sg = a.z >= 0.0f ? 1.0f : -1.0f;
+    return make_float3(sg * b.x, sg * b.y, sg * b.z);
+  }
+  const float f = a.z >= 0.0f ? f_rcp<P>(1.0f + a.z) : f_div<P>(1.0f - a.z, s2);
+  const float k = (a.x * b.y - a.y * b.x) * f;
+  return make_float3(b.x * a.z + a.x * b.z - a.y * k, b.y * a.z + a.y * b.z + a.x * k,
+                     b.z * a.z - (a.x * b.x + a.y * b.y));
+}
+
+// Direction from cos(theta) and the uniform of phi (sph_to_cart).
+template <bool P>
+__device__ __forceinline__ float3 dir_from_cos_u(float ct, float uphi) {
+  const float st = f_sqrt<P>(fmaxf(1.0f - ct * ct, 0.0f));
+  float sp, cp;
+  f_sincos_2pi<P>(uphi, &sp, &cp);
+  return make_float3(st * cp, st * sp, ct);
+}
+
+// ---- tables ------------------------------------------------------------------
+// Inverse-CDF spectrum sampled like a 1-D linear-filtered texture with
+// normalised coordinates and clamp addressing (src/spectrum.jl:79-83,
+// :137-138): texel i sits at (i + 0.5) / n.  FP32 weights instead of the
+// texture unit's 8-bit fraction.
+__device__ __forceinline__ float spectrum_sample(const float* __restrict__ k, int n, float u) {
+  if (n <= 1) return __ldg(k);
+  float x = fminf(fmaxf(u * (float)n - 0.5f, 0.0f), (float)(n - 1));
+  int i = min((int)x, n - 2);
+  float f = x - (float)i;
+  float a = __ldg(k + i), b = __ldg(k + i + 1);
+  return a + f * (b - a);
+}
+
+// Quantile table with knots at u = i / (n - 1).
+__device__ __forceinline__ float quantile_sample(const float* __restrict__ q, int n, float u) {
+  if (n <= 1) return __ldg(q);
+  float x = u * (float)(n - 1);
+  int i = min(max((int)x, 0), n - 2);
+  float f = x - (float)i;
+  float a = __ldg(q + i), b = __ldg(q + i + 1);
+  return a + f * (b - a);
+}
+
+// Medium at wavelength wl: {sca_len, group velocity, abs_len, n}, linear in wl.
+__device__ __forceinline__ float4 medium_at(const float4* __restrict__ t, int n, float wl_min,
+                                            float inv_step, float wl) {
+  float x = fminf(fmaxf((wl - wl_min) * inv_step, 0.0f), (float)(n - 1));
+  int i = min((int)x, n - 2);
+  float f = x - (float)i;
+  float4 a = __ldg(t + i), b = __ldg(t + i + 1);
+  return make_float4(a.x + f * (b.x - a.x), a.y + f * (b.y - a.y), a.z + f * (b.z - a.z),
+                     a.w + f * (b.w - a.w));
+}
+
+// ---- scattering (update_direction, src/photon_prop_cuda.jl:280-298) ---------
+// MixedHGES: with probability hg_weight Henyey-Greenstein at g, else
+// Einstein-Smoluchowski at b (Cardano root of the cubic CDF).  Both samples are
+// computed and one is selected (a warp almost always needs both anyway).
+template <bool P>
+__device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_choice, float eta) {
+  const float t = ph.hg_1mg2 * f_rcp<P>(fmaf(ph.hg_g, 2.0f * eta - 1.0f, 1.0f));
+  const float hg = fminf(fmaxf((ph.hg_1pg2 - t * t) * ph.hg_inv2g, -1.0f), 1.0f);
+  const float q = ph.es_k1 * (eta - 0.5f);
+  const float d = f_sqrt<P>(fmaf(q, q, ph.es_k2));
+  const float es = f_cbrt_pos<P>(q + d) - f_cbrt_pos<P>(d - q);
+  return u_choice < ph.hg_weight ? hg : es;
+}
+
+template <bool P>
+__device__ __forceinline__ float3 update_direction(const pp::PhaseDev& ph, float3 dir, float u1,
+                                                   float u2, float u3) {
+  const float c = scatter_cos<P>(ph, u1, u2);
+  return rot_from_ez<P>(dir, dir_from_cos_u<P>(c, u3));
+}
+
+// ---- ray-sphere test (_intersect_nsphere, src/photon_prop_cuda.jl:309-343) --
+// Hit iff the near intersection lies strictly inside (0, step).
+template <bool P>
+__device__ __forceinline__ bool sphere_hit(float4 s, float3 pos, float3 dir, float step,
+                                           float* d_out) {
+  const float dx = pos.x - s.x, dy = pos.y - s.y, dz = pos.z - s.z;
+  const float a = dir.x * dx + dir.y * dy + dir.z * dz;
+  const float pp = dx * dx + dy * dy + dz * dz;
+  const float b = a * a - (pp - s.w);
+  if (b >= 0.0f) {
+    const float d = -a - f_sqrt<P>(b);
+    if (d > 0.0f && d < step) {
+      *d_out = d;
+      return true;
+    }
+  }
+  return false;
+}
+
+// First target in index order intersected within (0, step): the candidates
+// come from a 3-D DDA walk over the uniform grid cells the segment crosses
+// (Amanatides & Woo); among all intersected candidates the smallest index
+// wins, which is exactly the reference's "first target in index order"
+// (src/photon_prop_cuda.jl:497-506).  Returns the 0-based index or -1.
+template <bool P>
+__device__ __forceinline__ int first_hit(const pp::GridDev& g, const uint32_t* __restrict__ cells,
+                                         const uint16_t* __restrict__ items,
+                                         const float4* __restrict__ sph, float3 pos, float3 dir,
+                                         float step, float* d_out) {
+  // Reciprocal direction with zero components pushed to a huge finite value.
+  const float ix = f_rcp<P>(fabsf(dir.x) > 1e-20f ? dir.x : copysignf(1e-20f, dir.x));
+  const float iy = f_rcp<P>(fabsf(dir.y) > 1e-20f ? dir.y : copysignf(1e-20f, dir.y));
+  const float iz = f_rcp<P>(fabsf(dir.z) > 1e-20f ? dir.z : copysignf(1e-20f, dir.z));
+  // Clip the segment to the grid box (slab test).
+  const float tx0 = (g.lo[0] - pos.x) * ix, tx1 = (g.hi[0] - pos.x) * ix;
+  const float ty0 = (g.lo[1] - pos.y) * iy, ty1 = (g.hi[1] - pos.y) * iy;
+  const float tz0 = (g.lo[2] - pos.z) * iz, tz1 = (g.hi[2] - pos.z) * iz;
+  const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+  const float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), step));
+  if (!(tmin <= tmax)) return -1;
+
+  const int nx = g.dims[0], ny = g.dims[1], nz = g.dims[2];
+  int cx = (int)floorf((fmaf(dir.x, tmin, pos.x) - g.lo[0]) * g.inv_cell[0]);
+  int cy = (int)floorf((fmaf(dir.y, tmin, pos.y) - g.lo[1]) * g.inv_cell[1]);
+  int cz = (int)floorf((fmaf(dir.z, tmin, pos.z) - g.lo[2]) * g.inv_cell[2]);
+  cx = min(max(cx, 0), nx - 1);
+  cy = min(max(cy, 0), ny - 1);
+  cz = min(max(cz, 0), nz - 1);
+  const int sx = dir.x >= 0.0f ? 1 : -1;
+  const int sy = dir.y >= 0.0f ? 1 : -1;
+  const int sz = dir.z >= 0.0f ? 1 : -1;
+  float tnx = (fmaf((float)(cx + (sx > 0)), g.cell[0], g.lo[0]) - pos.x) * ix;
+  float tny = (fmaf((float)(cy + (sy > 0)), g.cell[1], g.lo[1]) - pos.y) * iy;
+  float tnz = (fmaf((float)(cz + (sz > 0)), g.cell[2], g.lo[2]) - pos.z) * iz;
+  const float tdx = g.cell[0] * fabsf(ix);
+  const float tdy = g.cell[1] * fabsf(iy);
+  const float tdz = g.cell[2] * fabsf(iz);
+  const int strx = sx, stry = sy * nx, strz = sz * nx * ny;
+  int cidx = (cz * ny + cy) * nx + cx;
+
+  int best = 0x7fffffff;
+  float best_d = 0.0f;
+  const int max_iter = nx + ny + nz + 3;
+  for (int it = 0; it < max_iter; ++it) {
+    const uint32_t w = cells[cidx];
+    const uint32_t cnt = w >> pp::kCellStartBits;
+    if (cnt) {
+      const uint32_t first = w & pp::kCellStartMask;
+      for (uint32_t k = 0; k < cnt; ++k) {
+        const int j = items[first + k];
+        float d;
+        if (j < best && sphere_hit<P>(sph[j], pos, dir, step, &d)) {
+          best = j;
+          best_d = d;
+        }
+      }
+    }
+    if (tnx <= tny && tnx <= tnz) {
+      if (tnx > tmax) break;
+      cx += sx;
+      if ((unsigned)cx >= (unsigned)nx) break;
+      tnx += tdx;
+      cidx += strx;
+    } else if (tny <= tnz) {
+      if (tny > tmax) break;
+      cy += sy;
+      if ((unsigned)cy >= (unsigned)ny) break;
+      tny += tdy;
+      cidx += stry;
+    } else {
+      if (tnz > tmax) break;
+      cz += sz;
+      if ((unsigned)cz >= (unsigned)nz) break;
+      tnz += tdz;
+      cidx += strz;
+    }
+  }
+  if (best == 0x7fffffff) return -1;
+  *d_out = best_d;
+  return best;
+}
+
+// ---- emitters (initialize_photon_state, src/photon_prop_cuda.jl:158-276) ----
+
+// Gamma(shape, scale) by Marsaglia & Tsang (2000) from the photon's emitter
+// stream (rand_gamma, PhysicsTools; called at :214).
+template <bool P>
+__device__ __forceinline__ float gamma_sample(float shape, float scale, uint32_t plo, uint32_t phi,
+                                              uint32_t src, uint32_t k0, uint32_t k1) {
+  float a = shape;
+  const bool boost = a < 1.0f;
+  if (boost) a += 1.0f;
+  const float d = a - 1.0f / 3.0f;
+  const float c = P ? 1.0f / sqrtf(9.0f * d) : rsqrtf(9.0f * d);
+  for (int j = 0; j < kGammaMaxTries; ++j) {
+    const uint4 r = philox(make_uint4(plo, phi, kExtraCall + (uint32_t)j, src), k0, k1);
+    const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z);
+    float sn, cs;
+    f_sincos_2pi<P>(u1, &sn, &cs);
+    const float x = f_sqrt<P>(-2.0f * f_log<P>(u0)) * cs;
+    float v = fmaf(c, x, 1.0f);
+    if (v <= 0.0f) continue;
+    v = v * v * v;
+    const float x2 = x * x;
+    if (u2 < 1.0f - 0.0331f * x2 * x2 || f_log<P>(u2) < 0.5f * x2 + d * (1.0f - v + f_log<P>(v))) {
+      float gs = d * v;
+      if (boost) gs *= (P ? powf(u01(r.w), 1.0f / shape) : f_exp<P>(f_log<P>(u01(r.w)) / shape));
+      return gs * scale;
+    }
+  }
+  return d * scale;
+}
+
+// Cherenkov cone about the emitter axis: theta_c = acos(1/n), phi ~ U(0, 2pi),
+// optionally rotated onto a sampled track direction first
+// (sample_cherenkov_direction, :80-111).
+template <bool P>
+__device__ __forceinline__ float3 cherenkov_dir(float3 axis, float ref_ix, float u_phi,
+                                                float u_track, float u_track_phi, bool smear,
+                                                const float* __restrict__ track, int n_track) {
+  float3 ph = dir_from_cos_u<P>(f_rcp<P>(ref_ix), u_phi);
+  if (smear) {
+    const float ct = fminf(fmaxf(quantile_sample(track, n_track, u_track), -1.0f), 1.0f);
+    ph = rot_from_ez<P>(dir_from_cos_u<P>(ct, u_track_phi), ph);
+  }
+  return rot_from_ez<P>(axis, ph);
+}
+
+}  // namespace ppdev

@@ -1,0 +1,111 @@
+// pp_internal.h -- structures shared by the host runtime and the device
+// kernels of the photon-transport library (not part of the public ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pp_gb300.h"
+
+namespace pp {
+
+// Uniform culling grid over the targets.  The grid, its per-cell candidate
+// lists and the sphere table live in one contiguous 16-byte aligned "blob"
+// that each CTA stages into shared memory with one TMA bulk copy:
+//   [cells  : uint32 x n_cells, (count << 20) | first_item]  padded to 16 B
+//   [items  : uint16 x n_items, target indices]             padded to 16 B
+//   [spheres: float4 x n_targets, (x, y, z, r^2)]
+struct GridDev {
+  float lo[3];        // origin of cell (0,0,0)
+  float hi[3];        // lo + dims * cell
+  float cell[3];      // cell edge per axis (m)
+  float inv_cell[3];  // 1 / cell
+  int dims[3];
+  int n_cells;
+  int n_targets;
+  uint32_t off_items;    // byte offset of the item list in the blob
+  uint32_t off_spheres;  // byte offset of the sphere table in the blob
+  uint32_t blob_bytes;   // multiple of 16
+};
+
+constexpr uint32_t kCellStartBits = 20;                    // first item index
+constexpr uint32_t kCellStartMask = (1u << kCellStartBits) - 1u;
+constexpr uint32_t kCellMaxCount = (1u << (32 - kCellStartBits)) - 1u;
+constexpr float kGridMargin = 0.01f;                       // m, AABB inflation
+
+// Phase-function constants derived once per medium.
+struct PhaseDev {
+  float hg_weight;  // P(Henyey-Greenstein)
+  float hg_g;
+  float hg_1mg2;    // 1 - g^2
+  float hg_1pg2;    // 1 + g^2
+  float hg_inv2g;   // 1 / (2 g)
+  float es_k1;      // (b + 3) / b
+  float es_k2;      // 1 / b^3
+  float pad;
+};
+
+// Everything one launch of the propagation kernel needs (kernel parameter,
+// passed as __grid_constant__).
+struct LaunchArgs {
+  const pp_source* sources;
+  const unsigned long long* chunk_prefix;  // [n_src + 1] cumulative chunks
+  const long long* src_photons;            // [n_src] photons after scaling
+  unsigned long long total_chunks;
+  int n_src;
+  int chunk_photons;                       // 32 * photons_per_thread
+
+  const unsigned char* blob;               // grid blob (global memory)
+  GridDev grid;
+
+  const float4* medium;                    // {sca_len, v_group, abs_len, n}
+  int n_medium;
+  float med_wl_min;
+  float med_inv_step;
+  PhaseDev phase;
+
+  const float* spectrum;                   // inverse CDF knots or nullptr
+  int n_spectrum;
+  float mono_wavelength;
+  const float* track;                      // cos(theta) quantiles or nullptr
+  int n_track;
+
+  uint32_t key0, key1;                     // Philox key = seed
+  int n_steps;
+
+  pp_hit_record* hits;
+  unsigned long long capacity;
+  pp_counters* counters;
+  unsigned long long wait_limit_ns;        // bound on the TMA staging wait
+};
+
+// Host-side launch of the propagation kernel (pp_propagate.cu).
+cudaError_t launch_propagate(const LaunchArgs& args, int block_threads, int ctas_per_sm,
+                             bool precise, bool smem_grid, int num_sms, cudaStream_t stream,
+                             int* grid_out);
+// Maximum dynamic shared memory the kernel may use for the staged blob.
+size_t max_smem_blob_bytes();
+// Resident CTAs per SM for a configuration (occupancy calculator).
+int propagate_occupancy(int block_threads, bool precise, bool smem_grid, size_t smem_bytes);
+
+// Grid build on the device (pp_grid.cu).  targets_dev: n spheres in device
+// memory.  Returns 0 on success; *blob_out is allocated with cudaMalloc.
+int build_grid(const pp_sphere* targets_dev, int n, float cell_size, cudaStream_t stream,
+               GridDev* grid_out, unsigned char** blob_out, long long* n_items_out,
+               std::string* err);
+
+// Scatter hit records into columns on the device (pp_grid.cu).
+cudaError_t launch_hits_to_columns(const pp_hit_record* rec, long long n, const pp_hits& out,
+                                   cudaStream_t stream);
+
+// Philox on the device for the ABI diagnostic (pp_grid.cu).
+cudaError_t launch_debug_philox(const uint32_t* ctr, int n, uint32_t k0, uint32_t k1,
+                                uint32_t* out, cudaStream_t stream);
+
+// FFMA throughput kernel (pp_grid.cu); returns flops per launch.
+cudaError_t launch_fp32_peak(float* sink, int blocks, int threads, int iters, cudaStream_t stream);
+
+}  // namespace pp

@@ -1,0 +1,84 @@
+"""PhotonPropSetup (mirrors src/photon_propagation_setup.jl:9-25)."""
+from __future__ import annotations
+
+import numpy as np
+
+from . import sources as _sources
+from . import targets as _targets
+from .spectrum import InterpolatedSpectralDist, Monochromatic, SpectralDist, Spectrum
+
+# Medium tables are sampled on a 0.125 nm grid: linear interpolation of the
+# Kopelevich scattering length is then exact to about 2e-7 relative.
+MEDIUM_TABLE_STEP_NM = 0.125
+
+
+class PhotonPropSetup:
+    """Sources, targets, medium, spectrum and seed of one propagation.
+
+    ``PhotonPropSetup(sources, targets, medium, spectrum, seed;
+    photon_scaling=1., spectrum_interp_steps=600)`` as in the reference.  The
+    spectrum may be a ``Spectrum`` (as the reference requires) or, as in the
+    reference README, a bare ``Monochromatic``/``InterpolatedSpectralDist``.
+    ``track_smear`` optionally overrides the cos(theta) quantile table of the
+    Cherenkov track direction.
+    """
+
+    def __init__(self, sources, targets, medium, spectrum, seed, photon_scaling=1.0,
+                 spectrum_interp_steps=600, track_smear=None):
+        self.sources = list(sources)
+        self.targets = list(targets)
+        self.medium = medium
+        if isinstance(spectrum, Spectrum):
+            dist = spectrum.spectral_dist
+        elif isinstance(spectrum, SpectralDist):
+            dist = spectrum
+        else:
+            raise TypeError(f"unsupported spectrum {type(spectrum)}")
+        self.spec_dist = dist
+        if isinstance(dist, InterpolatedSpectralDist):
+            self.spectrum_knots = dist.device_knots(spectrum_interp_steps)
+            self.mono_wavelength = None
+        elif isinstance(dist, Monochromatic):
+            self.spectrum_knots = None
+            self.mono_wavelength = float(np.float32(dist.wavelength))
+        else:
+            raise TypeError(f"unsupported spectral distribution {type(dist)}")
+        self.seed = int(seed)
+        self.photon_scaling = float(photon_scaling)
+        self._track = None if track_smear is None else np.asarray(track_smear, np.float32)
+
+    # -- derived device inputs ------------------------------------------------
+    def wavelength_range(self):
+        if self.spectrum_knots is not None:
+            return float(self.spectrum_knots.min()), float(self.spectrum_knots.max())
+        return self.mono_wavelength, self.mono_wavelength
+
+    def medium_tables(self):
+        lo, hi = self.wavelength_range()
+        return self.medium.tables(lo, hi, MEDIUM_TABLE_STEP_NM)
+
+    def needs_track_smear(self) -> bool:
+        return any(s.kind in _sources.TRACK_SMEAR_KINDS for s in self.sources)
+
+    def track_quantiles(self):
+        if self._track is None:
+            from .track_smear import beta_track_quantiles
+            self._track = beta_track_quantiles()
+        return self._track
+
+    def source_records(self):
+        return _sources.to_records(self.sources)
+
+    def sphere_records(self):
+        return _targets.to_spheres(self.targets)
+
+    def upload(self, ctx, cell_size: float = 0.0) -> None:
+        """Send medium, spectrum, track table and targets to a Context."""
+        ctx.set_medium(self.medium_tables())
+        if self.spectrum_knots is not None:
+            ctx.set_spectrum(self.spectrum_knots)
+        else:
+            ctx.set_monochromatic(self.mono_wavelength)
+        if self.needs_track_smear():
+            ctx.set_track_smear(self.track_quantiles())
+        ctx.set_targets(self.sphere_records(), len(self.targets), cell_size)
