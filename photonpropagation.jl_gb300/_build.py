@@ -22,8 +22,10 @@ LIB = os.path.join(OUT_DIR, "libpp_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-              "--expt-relaxed-constexpr"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler",
+              "-fPIC,-fvisibility=hidden,-ffp-contract=off", "--expt-relaxed-constexpr"]
+# Per-file flags: the replay kernel must not contract a*b+c into FMAs.
+FILE_FLAGS = {"pp_propagate_precise.cu": ["-fmad=false"]}
 
 
 def nvcc_path() -> str:
@@ -59,7 +61,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     def compile_one(src):
         obj = os.path.join(OBJ_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-c", src, "-o", obj]
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-I",
+               INCLUDE, "-c", src, "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -390,6 +390,7 @@ PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
   const float b = m->es_b > 0.0f ? m->es_b : 1.0f;
   p.es_k1 = (b + 3.0f) / b;
   p.es_k2 = 1.0f / (b * b * b);
+  p.es_b = b;
   ctx->has_medium = true;
   ctx->version++;
   return PP_OK;

@@ -114,11 +114,21 @@ __device__ __forceinline__ void f_sincos(float x, float* s, float* c) {
   if (P) sincosf(x, s, c); else __sincosf(x, s, c);
 }
 
+// a*b + c: fused in the fast variant, two roundings in the replay variant
+// (which is compiled without contraction, like the oracle).
+template <bool P>
+__device__ __forceinline__ float madd(float a, float b, float c) {
+  return P ? a * b + c : fmaf(a, b, c);
+}
+
+// uniform(minval, maxval) of src/photon_prop_cuda.jl:48-51 on a given uniform.
+__device__ __forceinline__ float uniform_ab(float a, float b, float u) { return a + u * (b - a); }
+
 // ---- geometry ----------------------------------------------------------------
 // Rotation taking e_z onto the unit vector a, applied to b (rot_from_ez_fast,
 // PhysicsTools; called at src/photon_prop_cuda.jl:92-95, :296).  Written in
 // the Rodrigues form whose only division is well conditioned in each
-// hemisphere of a.
+// hemisphere of a; the expression order matches the oracle's.
 template <bool P>
 __device__ __forceinline__ float3 rot_from_ez(float3 a, float3 b) {
   const float s2 = a.x * a.x + a.y * a.y;
@@ -132,12 +142,30 @@ __device__ __forceinline__ float3 rot_from_ez(float3 a, float3 b) {
                      b.z * a.z - (a.x * b.x + a.y * b.y));
 }
 
-// Direction from cos(theta) and the uniform of phi (sph_to_cart).
+// sph_to_cart(theta, phi) with phi = 2*pi*u_phi.
 template <bool P>
-__device__ __forceinline__ float3 dir_from_cos_u(float ct, float uphi) {
-  const float st = f_sqrt<P>(fmaxf(1.0f - ct * ct, 0.0f));
+__device__ __forceinline__ float3 sph_to_cart(float theta, float u_phi) {
+  if (P) {
+    const float phi = uniform_ab(0.0f, kTwoPi, u_phi);
+    const float st = sinf(theta), ct = cosf(theta);
+    return make_float3(st * cosf(phi), st * sinf(phi), ct);
+  }
+  float st, ct, sp, cp;
+  __sincosf(theta, &st, &ct);
+  f_sincos_2pi<false>(u_phi, &sp, &cp);
+  return make_float3(st * cp, st * sp, ct);
+}
+
+// Direction with polar cosine ct and azimuth 2*pi*u_phi.  The replay variant
+// goes through theta = acos(ct) as the reference does
+// (initialize_direction_isotropic, src/photon_prop_cuda.jl:73-77); the fast
+// one uses sin(theta) = sqrt(1 - ct^2).
+template <bool P>
+__device__ __forceinline__ float3 dir_from_cos(float ct, float u_phi) {
+  if (P) return sph_to_cart<true>(acosf(ct), u_phi);
+  const float st = approx_sqrt(fmaxf(1.0f - ct * ct, 0.0f));
   float sp, cp;
-  f_sincos_2pi<P>(uphi, &sp, &cp);
+  f_sincos_2pi<false>(u_phi, &sp, &cp);
   return make_float3(st * cp, st * sp, ct);
 }
 
@@ -148,45 +176,56 @@ __device__ __forceinline__ float3 dir_from_cos_u(float ct, float uphi) {
 // texture unit's 8-bit fraction.
 __device__ __forceinline__ float spectrum_sample(const float* __restrict__ k, int n, float u) {
   if (n <= 1) return __ldg(k);
-  float x = fminf(fmaxf(u * (float)n - 0.5f, 0.0f), (float)(n - 1));
-  int i = min((int)x, n - 2);
-  float f = x - (float)i;
-  float a = __ldg(k + i), b = __ldg(k + i + 1);
+  const float x = fminf(fmaxf(u * (float)n - 0.5f, 0.0f), (float)(n - 1));
+  const int i = min((int)x, n - 2);
+  const float f = x - (float)i;
+  const float a = __ldg(k + i), b = __ldg(k + i + 1);
   return a + f * (b - a);
 }
 
 // Quantile table with knots at u = i / (n - 1).
 __device__ __forceinline__ float quantile_sample(const float* __restrict__ q, int n, float u) {
   if (n <= 1) return __ldg(q);
-  float x = u * (float)(n - 1);
-  int i = min(max((int)x, 0), n - 2);
-  float f = x - (float)i;
-  float a = __ldg(q + i), b = __ldg(q + i + 1);
+  const float x = u * (float)(n - 1);
+  const int i = min(max((int)x, 0), n - 2);
+  const float f = x - (float)i;
+  const float a = __ldg(q + i), b = __ldg(q + i + 1);
   return a + f * (b - a);
 }
 
 // Medium at wavelength wl: {sca_len, group velocity, abs_len, n}, linear in wl.
 __device__ __forceinline__ float4 medium_at(const float4* __restrict__ t, int n, float wl_min,
                                             float inv_step, float wl) {
-  float x = fminf(fmaxf((wl - wl_min) * inv_step, 0.0f), (float)(n - 1));
-  int i = min((int)x, n - 2);
-  float f = x - (float)i;
-  float4 a = __ldg(t + i), b = __ldg(t + i + 1);
+  const float x = fminf(fmaxf((wl - wl_min) * inv_step, 0.0f), (float)(n - 1));
+  const int i = min((int)x, n - 2);
+  const float f = x - (float)i;
+  const float4 a = __ldg(t + i), b = __ldg(t + i + 1);
   return make_float4(a.x + f * (b.x - a.x), a.y + f * (b.y - a.y), a.z + f * (b.z - a.z),
                      a.w + f * (b.w - a.w));
 }
 
 // ---- scattering (update_direction, src/photon_prop_cuda.jl:280-298) ---------
 // MixedHGES: with probability hg_weight Henyey-Greenstein at g, else
-// Einstein-Smoluchowski at b (Cardano root of the cubic CDF).  Both samples are
-// computed and one is selected (a warp almost always needs both anyway).
+// Einstein-Smoluchowski at b (Cardano root of the cubic CDF).  Both samples
+// are computed and one is selected (a warp almost always needs both anyway).
 template <bool P>
 __device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_choice, float eta) {
-  const float t = ph.hg_1mg2 * f_rcp<P>(fmaf(ph.hg_g, 2.0f * eta - 1.0f, 1.0f));
-  const float hg = fminf(fmaxf((ph.hg_1pg2 - t * t) * ph.hg_inv2g, -1.0f), 1.0f);
-  const float q = ph.es_k1 * (eta - 0.5f);
-  const float d = f_sqrt<P>(fmaf(q, q, ph.es_k2));
-  const float es = f_cbrt_pos<P>(q + d) - f_cbrt_pos<P>(d - q);
+  float hg, es;
+  if (P) {  // the oracle's expression forms, IEEE division/sqrt/cbrt
+    const float g = ph.hg_g, b = ph.es_b;
+    const float t = (1.0f - g * g) / (1.0f + g * (2.0f * eta - 1.0f));
+    hg = 1.0f / (2.0f * g) * (1.0f + g * g - t * t);
+    hg = hg < -1.0f ? -1.0f : (hg > 1.0f ? 1.0f : hg);
+    const float q = (b + 3.0f) * (eta - 0.5f) / b;
+    const float d = sqrtf(q * q + 1.0f / (b * b * b));
+    es = cbrtf(q + d) + cbrtf(q - d);
+  } else {
+    const float t = ph.hg_1mg2 * approx_rcp(fmaf(ph.hg_g, 2.0f * eta - 1.0f, 1.0f));
+    hg = fminf(fmaxf((ph.hg_1pg2 - t * t) * ph.hg_inv2g, -1.0f), 1.0f);
+    const float q = ph.es_k1 * (eta - 0.5f);
+    const float d = approx_sqrt(fmaf(q, q, ph.es_k2));
+    es = f_cbrt_pos<false>(q + d) - f_cbrt_pos<false>(d - q);
+  }
   return u_choice < ph.hg_weight ? hg : es;
 }
 
@@ -194,7 +233,17 @@ template <bool P>
 __device__ __forceinline__ float3 update_direction(const pp::PhaseDev& ph, float3 dir, float u1,
                                                    float u2, float u3) {
   const float c = scatter_cos<P>(ph, u1, u2);
-  return rot_from_ez<P>(dir, dir_from_cos_u<P>(c, u3));
+  const float s2 = 1.0f - c * c;
+  const float st = f_sqrt<P>(s2 > 0.0f ? s2 : 0.0f);
+  float sp, cp;
+  if (P) {
+    const float phi = uniform_ab(0.0f, kTwoPi, u3);
+    sp = sinf(phi);
+    cp = cosf(phi);
+  } else {
+    f_sincos_2pi<false>(u3, &sp, &cp);
+  }
+  return rot_from_ez<P>(dir, make_float3(cp * st, sp * st, c));
 }
 
 // ---- ray-sphere test (_intersect_nsphere, src/photon_prop_cuda.jl:309-343) --
@@ -226,10 +275,11 @@ __device__ __forceinline__ int first_hit(const pp::GridDev& g, const uint32_t* _
                                          const uint16_t* __restrict__ items,
                                          const float4* __restrict__ sph, float3 pos, float3 dir,
                                          float step, float* d_out) {
-  // Reciprocal direction with zero components pushed to a huge finite value.
-  const float ix = f_rcp<P>(fabsf(dir.x) > 1e-20f ? dir.x : copysignf(1e-20f, dir.x));
-  const float iy = f_rcp<P>(fabsf(dir.y) > 1e-20f ? dir.y : copysignf(1e-20f, dir.y));
-  const float iz = f_rcp<P>(fabsf(dir.z) > 1e-20f ? dir.z : copysignf(1e-20f, dir.z));
+  // Reciprocal direction; zero components become a huge value of the same
+  // sign as the step direction chosen below (+ for +0 and -0 alike).
+  const float ix = approx_rcp(fabsf(dir.x) > 1e-20f ? dir.x : 1e-20f);
+  const float iy = approx_rcp(fabsf(dir.y) > 1e-20f ? dir.y : 1e-20f);
+  const float iz = approx_rcp(fabsf(dir.z) > 1e-20f ? dir.z : 1e-20f);
   // Clip the segment to the grid box (slab test).
   const float tx0 = (g.lo[0] - pos.x) * ix, tx1 = (g.hi[0] - pos.x) * ix;
   const float ty0 = (g.lo[1] - pos.y) * iy, ty1 = (g.hi[1] - pos.y) * iy;
@@ -245,9 +295,9 @@ __device__ __forceinline__ int first_hit(const pp::GridDev& g, const uint32_t* _
   cx = min(max(cx, 0), nx - 1);
   cy = min(max(cy, 0), ny - 1);
   cz = min(max(cz, 0), nz - 1);
-  const int sx = dir.x >= 0.0f ? 1 : -1;
-  const int sy = dir.y >= 0.0f ? 1 : -1;
-  const int sz = dir.z >= 0.0f ? 1 : -1;
+  const int sx = ix >= 0.0f ? 1 : -1;
+  const int sy = iy >= 0.0f ? 1 : -1;
+  const int sz = iz >= 0.0f ? 1 : -1;
   float tnx = (fmaf((float)(cx + (sx > 0)), g.cell[0], g.lo[0]) - pos.x) * ix;
   float tny = (fmaf((float)(cy + (sy > 0)), g.cell[1], g.lo[1]) - pos.y) * iy;
   float tnz = (fmaf((float)(cz + (sz > 0)), g.cell[2], g.lo[2]) - pos.z) * iz;
@@ -314,16 +364,21 @@ __device__ __forceinline__ float gamma_sample(float shape, float scale, uint32_t
   for (int j = 0; j < kGammaMaxTries; ++j) {
     const uint4 r = philox(make_uint4(plo, phi, kExtraCall + (uint32_t)j, src), k0, k1);
     const float u0 = u01(r.x), u1 = u01(r.y), u2 = u01(r.z);
-    float sn, cs;
-    f_sincos_2pi<P>(u1, &sn, &cs);
+    float cs;
+    if (P) {
+      cs = cosf(kTwoPi * u1);
+    } else {
+      float sn;
+      f_sincos_2pi<false>(u1, &sn, &cs);
+    }
     const float x = f_sqrt<P>(-2.0f * f_log<P>(u0)) * cs;
-    float v = fmaf(c, x, 1.0f);
+    float v = 1.0f + c * x;
     if (v <= 0.0f) continue;
     v = v * v * v;
     const float x2 = x * x;
     if (u2 < 1.0f - 0.0331f * x2 * x2 || f_log<P>(u2) < 0.5f * x2 + d * (1.0f - v + f_log<P>(v))) {
       float gs = d * v;
-      if (boost) gs *= (P ? powf(u01(r.w), 1.0f / shape) : f_exp<P>(f_log<P>(u01(r.w)) / shape));
+      if (boost) gs *= (P ? powf(u01(r.w), 1.0f / shape) : f_exp<false>(f_log<false>(u01(r.w)) / shape));
       return gs * scale;
     }
   }
@@ -337,10 +392,12 @@ template <bool P>
 __device__ __forceinline__ float3 cherenkov_dir(float3 axis, float ref_ix, float u_phi,
                                                 float u_track, float u_track_phi, bool smear,
                                                 const float* __restrict__ track, int n_track) {
-  float3 ph = dir_from_cos_u<P>(f_rcp<P>(ref_ix), u_phi);
+  float3 ph = P ? sph_to_cart<true>(acosf(1.0f / ref_ix), u_phi)
+                : dir_from_cos<false>(approx_rcp(ref_ix), u_phi);
   if (smear) {
-    const float ct = fminf(fmaxf(quantile_sample(track, n_track, u_track), -1.0f), 1.0f);
-    ph = rot_from_ez<P>(dir_from_cos_u<P>(ct, u_track_phi), ph);
+    float ct = quantile_sample(track, n_track, u_track);
+    ct = ct > 1.0f ? 1.0f : (ct < -1.0f ? -1.0f : ct);
+    ph = rot_from_ez<P>(dir_from_cos<P>(ct, u_track_phi), ph);
   }
   return rot_from_ez<P>(axis, ph);
 }

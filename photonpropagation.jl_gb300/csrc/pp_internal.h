@@ -45,7 +45,7 @@ struct PhaseDev {
   float hg_inv2g;   // 1 / (2 g)
   float es_k1;      // (b + 3) / b
   float es_k2;      // 1 / b^3
-  float pad;
+  float es_b;       // Einstein-Smoluchowski b
 };
 
 // Everything one launch of the propagation kernel needs (kernel parameter,

@@ -1,302 +1,19 @@
-// pp_propagate.cu -- the persistent photon-propagation kernel.
-//
-// Replaces cuda_propagate_photons! (PhotonPropagation.jl v0.9.3,
-// src/photon_prop_cuda.jl:429-549) and its one-launch-per-source host loop
-// (:927-943).  Design:
-//   * persistent CTAs (a multiple of the SM count); every warp pulls chunks of
-//     32 * photons_per_thread photons of one source from a device work queue,
-//     so one launch covers any number of sources with uneven photon counts;
-//   * photon i of source s draws its random numbers from Philox4x32-10 at
-//     counter (i, call, s) and key = seed, so results do not depend on the
-//     launch shape and any photon range can be replayed;
-//   * the target culling grid (cells, candidate lists, spheres) is staged
-//     once per CTA into shared memory with a TMA bulk copy (cp.async.bulk)
-//     completing on an mbarrier, waited on with a time bound;
-//   * hits are appended with one atomic per warp (warp-aggregated) into an
-//     80-byte record written as five 16-byte vector stores.
+// pp_propagate.cu -- fast variant of the propagation kernel and the host-side
+// launch (grid sizing from the occupancy calculator, dynamic shared memory for
+// the staged target grid).
 #include <cuda_runtime.h>
 
-#include "pp_device.cuh"
-#include "pp_internal.h"
+#include "pp_kernel.cuh"
 
 namespace pp {
+
+// Replay variant, instantiated in pp_propagate_precise.cu.
+const void* precise_kernel_ptr(bool smem_grid);
+
 namespace {
 
-using namespace ppdev;
-
-__device__ __forceinline__ unsigned long long global_timer_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ unsigned long long* u64(uint64_t* p) {
-  return reinterpret_cast<unsigned long long*>(p);
-}
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-// Stage `bytes` (multiple of 16, 16-byte aligned source) into shared memory
-// with TMA bulk copies that complete on one mbarrier.  Every thread then waits
-// on the barrier's phase 0 for at most limit_ns.  Returns false on timeout.
-__device__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_t bytes,
-                           unsigned long long* bar, unsigned long long limit_ns) {
-  const uint32_t bar_a = smem_addr(bar);
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar_a), "r"(1) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(bytes)
-                 : "memory");
-    constexpr uint32_t kChunk = 32768;
-    for (uint32_t off = 0; off < bytes; off += kChunk) {
-      const uint32_t n = bytes - off < kChunk ? bytes - off : kChunk;
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_addr(dst + off)),
-          "l"(src + off), "r"(n), "r"(bar_a)
-          : "memory");
-    }
-  }
-  const unsigned long long t0 = global_timer_ns();
-  while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(bar_a), "r"(0)
-        : "memory");
-    if (done) return true;
-    if (global_timer_ns() - t0 > limit_ns) return false;
-  }
-}
-
-// Append one hit: one atomic per warp for all lanes that hit in this step.
-__device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, float wl, float3 dir,
-                                           float dist, float3 idir, float abs_w, double time,
-                                           long long photon, int module_index, int n_steps,
-                                           int source_index, bool* overflowed) {
-  const unsigned act = __activemask();
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(act) - 1;
-  const unsigned rank = __popc(act & ((1u << lane) - 1u));
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(u64(&a.counters->n_hits), (unsigned long long)__popc(act));
-  base = __shfl_sync(act, base, leader);
-  const unsigned long long slot = base + rank;
-  if (slot < a.capacity) {
-    float4* r = reinterpret_cast<float4*>(a.hits + slot);
-    const double2 tp = make_double2(time, __longlong_as_double(photon));
-    r[0] = make_float4(pos.x, pos.y, pos.z, wl);
-    r[1] = make_float4(dir.x, dir.y, dir.z, dist);
-    r[2] = make_float4(idir.x, idir.y, idir.z, abs_w);
-    reinterpret_cast<double2*>(r)[3] = tp;
-    r[4] = make_float4(__int_as_float(module_index), __int_as_float(n_steps),
-                       __int_as_float(source_index), 0.0f);
-  } else {
-    atomicOr(&a.counters->err_flags, (unsigned)PP_FLAG_OVERFLOW);
-    *overflowed = true;
-  }
-}
-
-template <bool kPrecise, bool kSmemGrid>
-__global__ void propagate_kernel(const __grid_constant__ LaunchArgs a) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) unsigned long long bar;
-
-  const uint32_t* cells;
-  const uint16_t* items;
-  const float4* sph;
-  if (kSmemGrid) {
-    if (!stage_blob(smem, a.blob, a.grid.blob_bytes, &bar, a.wait_limit_ns)) {
-      atomicOr(&a.counters->err_flags, (unsigned)PP_FLAG_TIMEOUT);
-      return;
-    }
-    cells = reinterpret_cast<const uint32_t*>(smem);
-    items = reinterpret_cast<const uint16_t*>(smem + a.grid.off_items);
-    sph = reinterpret_cast<const float4*>(smem + a.grid.off_spheres);
-  } else {
-    cells = reinterpret_cast<const uint32_t*>(a.blob);
-    items = reinterpret_cast<const uint16_t*>(a.blob + a.grid.off_items);
-    sph = reinterpret_cast<const float4*>(a.blob + a.grid.off_spheres);
-  }
-  const bool have_grid = a.grid.n_targets > 0;
-
-  const int lane = threadIdx.x & 31;
-  unsigned long long steps_acc = 0, sim_acc = 0;
-
-  while (true) {
-    unsigned long long c = 0;
-    unsigned stop = 0;
-    if (lane == 0) {
-      c = atomicAdd(u64(&a.counters->work_next), 1ull);
-      stop = *reinterpret_cast<volatile unsigned*>(&a.counters->err_flags) & PP_FLAG_OVERFLOW;
-    }
-    c = __shfl_sync(0xffffffffu, c, 0);
-    stop = __shfl_sync(0xffffffffu, stop, 0);
-    if (c >= a.total_chunks || stop) break;
-
-    // Source owning chunk c: last s with chunk_prefix[s] <= c.
-    int lo = 0, hi = a.n_src;
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (__ldg(a.chunk_prefix + mid) <= c) lo = mid; else hi = mid;
-    }
-    const int s = lo;
-    const long long p0 = (long long)(c - __ldg(a.chunk_prefix + s)) * a.chunk_photons;
-    const long long pend = min(p0 + (long long)a.chunk_photons, __ldg(a.src_photons + s));
-    const pp_source* sp = a.sources + s;
-    const int kind = __ldg(&sp->kind);
-    const float3 spos = make_float3(__ldg(&sp->position[0]), __ldg(&sp->position[1]),
-                                    __ldg(&sp->position[2]));
-    const float3 saxis = make_float3(__ldg(&sp->direction[0]), __ldg(&sp->direction[1]),
-                                     __ldg(&sp->direction[2]));
-    const float stime = __ldg(&sp->time);
-    const long long first = __ldg(&sp->first_photon);
-
-    for (long long pl = p0 + lane; pl < pend; pl += 32) {
-      const long long p = first + pl;  // global photon index (RNG counter)
-      const uint32_t plo = (uint32_t)p, phi = (uint32_t)((unsigned long long)p >> 32);
-      const uint4 r0 = philox(make_uint4(plo, phi, 0u, (uint32_t)s), a.key0, a.key1);
-      const float u0 = u01(r0.x), u1 = u01(r0.y), u2 = u01(r0.z), u3 = u01(r0.w);
-      const float wl = a.spectrum ? spectrum_sample(a.spectrum, a.n_spectrum, u0)
-                                  : a.mono_wavelength;
-      const float4 med = medium_at(a.medium, a.n_medium, a.med_wl_min, a.med_inv_step, wl);
-
-      // ---- initial state (initialize_photon_state) ----
-      float3 pos = spos, dir;
-      float t0 = stime;
-      switch (kind) {
-        case PP_SRC_POINTLIKE_ISOTROPIC:
-        case PP_SRC_POINTLIKE_TIME_RANGE:
-          dir = dir_from_cos_u<kPrecise>(fmaf(u1, 2.0f, -1.0f), u2);
-          if (kind == PP_SRC_POINTLIKE_TIME_RANGE) t0 = stime + u3 * (__ldg(&sp->time_end) - stime);
-          break;
-        case PP_SRC_COLLIMATED_ISOTROPIC: {
-          const float cut = __ldg(&sp->cut_angle_cos);
-          dir = dir_from_cos_u<kPrecise>(cut + u2 * (1.0f - cut), u1);
-          break;
-        }
-        case PP_SRC_PENCIL: {
-          const float div = __ldg(&sp->beam_divergence);
-          if (div > 0.0f) {
-            const float th = f_sqrt<kPrecise>(u1 * (div * div));
-            float st, ct;
-            f_sincos<kPrecise>(th, &st, &ct);
-            float sp2, cp2;
-            f_sincos_2pi<kPrecise>(u2, &sp2, &cp2);
-            dir = rot_from_ez<kPrecise>(saxis, make_float3(st * cp2, st * sp2, ct));
-          } else {
-            dir = saxis;
-          }
-          break;
-        }
-        case PP_SRC_AXICONE: {
-          float th = __ldg(&sp->angle);
-          const float div = __ldg(&sp->beam_divergence);
-          if (div > 0.0f) {
-            float sn, cs;
-            f_sincos_2pi<kPrecise>(u3, &sn, &cs);
-            th += f_sqrt<kPrecise>(-2.0f * f_log<kPrecise>(u2)) * cs * div;
-          }
-          float st, ct;
-          f_sincos<kPrecise>(th, &st, &ct);
-          float sp2, cp2;
-          f_sincos_2pi<kPrecise>(u1, &sp2, &cp2);
-          dir = rot_from_ez<kPrecise>(saxis, make_float3(st * cp2, st * sp2, ct));
-          break;
-        }
-        case PP_SRC_EXTENDED_CHERENKOV:
-        case PP_SRC_EXTENDED_CHERENKOV_NOSMEAR:
-        case PP_SRC_POINTLIKE_CHERENKOV:
-        case PP_SRC_CHERENKOV_TRACK: {
-          float along = 0.0f;
-          if (kind == PP_SRC_EXTENDED_CHERENKOV || kind == PP_SRC_EXTENDED_CHERENKOV_NOSMEAR) {
-            along = gamma_sample<kPrecise>(__ldg(&sp->long_a), 1.0f / __ldg(&sp->long_b), plo, phi,
-                                           (uint32_t)s, a.key0, a.key1) *
-                    __ldg(&sp->long_lrad);
-          } else if (kind == PP_SRC_CHERENKOV_TRACK) {
-            const uint4 re = philox(make_uint4(plo, phi, kExtraCall, (uint32_t)s), a.key0, a.key1);
-            along = u01(re.x) * __ldg(&sp->length);
-          }
-          pos = make_float3(spos.x + along * saxis.x, spos.y + along * saxis.y,
-                            spos.z + along * saxis.z);
-          t0 = stime + along / kCVac;
-          dir = cherenkov_dir<kPrecise>(saxis, med.w, u1, u2, u3,
-                                        kind != PP_SRC_EXTENDED_CHERENKOV_NOSMEAR, a.track,
-                                        a.n_track);
-          break;
-        }
-        default:
-          dir = make_float3(0.0f, 0.0f, 1.0f);
-          break;
-      }
-
-      const float3 idir = dir;
-      const float sca_len = med.x;
-      float dist = 0.0f, comp = 0.0f;  // Kahan-compensated path length
-      bool overflowed = false;
-      int k = 1;
-      for (; k <= a.n_steps; ++k) {
-        const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.key0, a.key1);
-        const float step = -f_log<kPrecise>(u01(r.x)) * sca_len;
-        float d = 0.0f;
-        const int j = have_grid ? first_hit<kPrecise>(a.grid, cells, items, sph, pos, dir, step, &d)
-                                : -1;
-        if (j >= 0) {
-          pos = make_float3(fmaf(dir.x, d, pos.x), fmaf(dir.y, d, pos.y), fmaf(dir.z, d, pos.z));
-          {
-            const float y = d - comp, t = dist + y;
-            comp = (t - dist) - y;
-            dist = t;
-          }
-          const double dist_c = (double)dist - (double)comp;
-          const double time = (double)t0 + dist_c / (double)med.y;
-          const float dist_f = (float)dist_c;
-          const float abs_w = f_exp<kPrecise>(-f_div<kPrecise>(dist_f, med.z));
-          record_hit(a, pos, wl, dir, dist_f, idir, abs_w, time, p, j + 1, k, s, &overflowed);
-          break;
-        }
-        pos = make_float3(fmaf(dir.x, step, pos.x), fmaf(dir.y, step, pos.y),
-                          fmaf(dir.z, step, pos.z));
-        {
-          const float y = step - comp, t = dist + y;
-          comp = (t - dist) - y;
-          dist = t;
-        }
-        dir = update_direction<kPrecise>(a.phase, dir, u01(r.y), u01(r.z), u01(r.w));
-      }
-      steps_acc += (unsigned long long)min(k, a.n_steps);
-      if (!overflowed) sim_acc += 1;
-    }
-  }
-
-  // One atomic per warp for the photon and step counters.
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    steps_acc += __shfl_xor_sync(0xffffffffu, steps_acc, o);
-    sim_acc += __shfl_xor_sync(0xffffffffu, sim_acc, o);
-  }
-  if (lane == 0) {
-    atomicAdd(u64(&a.counters->photon_steps), steps_acc);
-    atomicAdd(u64(&a.counters->n_ph_sim), sim_acc);
-  }
-}
-
-template <bool P, bool S>
-const void* kernel_ptr() {
-  return reinterpret_cast<const void*>(&propagate_kernel<P, S>);
-}
-
 const void* select_kernel(bool precise, bool smem_grid) {
-  if (precise) return smem_grid ? kernel_ptr<true, true>() : kernel_ptr<true, false>();
+  if (precise) return precise_kernel_ptr(smem_grid);
   return smem_grid ? kernel_ptr<false, true>() : kernel_ptr<false, false>();
 }
 
