@@ -121,6 +121,8 @@ struct pp_ctx {
   pp_sphere* d_targets = nullptr;
   unsigned char* d_blob = nullptr;
   GridDev grid{};
+  unsigned char* d_safety = nullptr;
+  pp::SafetyDev sgrid{};
   long long n_items = 0;
   bool has_targets = false;
 
@@ -137,7 +139,7 @@ struct pp_ctx {
   bool has_sources = false;
   bool needs_track = false;
 
-  pp_tuning tuning{256, 8, 0, 0, 0.0f, 0, {0, 0}};
+  pp_tuning tuning{256, 8, 0, 0, 0.0f, 0, 0.0f, 0};
 
   // scratch of pp_propagate
   pp_hit_record* d_hits = nullptr;
@@ -208,6 +210,21 @@ int rebuild_grid(pp_ctx* ctx, float cell_size) {
   ctx->grid = g;
   ctx->d_blob = blob;
   ctx->n_items = n_items;
+  // Safety field over the same box; automatic cell: about 32k cells (32 KiB).
+  cudaFree(ctx->d_safety);
+  ctx->d_safety = nullptr;
+  float hs = ctx->tuning.safety_cell;
+  if (!(hs > 0.0f)) {
+    double vol = 1.0;
+    for (int a = 0; a < 3; ++a) vol *= std::max(1e-6, (double)g.hi[a] - (double)g.lo[a]);
+    hs = (float)std::max(1e-3, std::cbrt(vol / 32768.0));
+  }
+  pp::SafetyDev sg{};
+  unsigned char* field = nullptr;
+  if (pp::build_safety(ctx->d_targets, n, g, hs, ctx->stream, &sg, &field, &err) != 0)
+    return set_error(PP_ERR_CUDA, "pp_set_targets: %s", err.c_str());
+  ctx->sgrid = sg;
+  ctx->d_safety = field;
   ctx->version++;
   return PP_OK;
 }
@@ -224,8 +241,13 @@ int check_ready(const pp_ctx* ctx) {
   return PP_OK;
 }
 
+// Grid and safety field go to shared memory when two CTAs of the configured
+// size still fit on an SM; otherwise both are read from global memory.
 bool use_smem_grid(const pp_ctx* ctx) {
-  return !ctx->tuning.grid_in_global && ctx->grid.blob_bytes <= pp::max_smem_blob_bytes();
+  if (ctx->tuning.grid_in_global) return false;
+  return pp::propagate_smem_bytes(ctx->grid.blob_bytes, ctx->sgrid.bytes, true,
+                                  ctx->tuning.block_threads, nullptr, nullptr) <=
+         pp::kSmemPerCtaBudget;
 }
 
 LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_record* hits,
@@ -239,6 +261,8 @@ LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_reco
   a.chunk_photons = 32 * ctx->tuning.photons_per_thread;
   a.blob = ctx->d_blob;
   a.grid = ctx->grid;
+  a.safety = ctx->d_safety;
+  a.sgrid = ctx->sgrid;
   a.medium = ctx->d_medium;
   a.n_medium = ctx->n_medium;
   a.med_wl_min = ctx->med_wl_min;
@@ -275,7 +299,8 @@ int enqueue(pp_ctx* ctx, long long seed, int n_steps, pp_hit_record* d_hits, lon
 int validate_launch(pp_ctx* ctx, int n_steps, const void* d_hits, long long capacity,
                     const void* d_ctr) {
   if (!ctx) return set_error(PP_ERR_INVALID, "null context");
-  if (n_steps < 1) return set_error(PP_ERR_INVALID, "n_steps must be >= 1 (got %d)", n_steps);
+  if (n_steps < 1 || n_steps > 65535)
+    return set_error(PP_ERR_INVALID, "n_steps must be in [1, 65535] (got %d)", n_steps);
   if (!d_ctr) return set_error(PP_ERR_INVALID, "null counters pointer");
   if (capacity < 0) return set_error(PP_ERR_INVALID, "negative capacity");
   if (capacity > 0 && !d_hits) return set_error(PP_ERR_INVALID, "null hit buffer");
@@ -339,6 +364,7 @@ PP_API int pp_destroy(pp_ctx* ctx) {
   cudaFree(ctx->d_track);
   cudaFree(ctx->d_targets);
   cudaFree(ctx->d_blob);
+  cudaFree(ctx->d_safety);
   cudaFree(ctx->d_sources);
   cudaFree(ctx->d_prefix);
   cudaFree(ctx->d_src_photons);
@@ -495,14 +521,16 @@ PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float phot
 
 PP_API int pp_set_tuning(pp_ctx* ctx, const pp_tuning* t) {
   if (!ctx || !t) return set_error(PP_ERR_INVALID, "null argument");
-  if (t->block_threads < 64 || t->block_threads > 1024 || (t->block_threads % 32) != 0)
-    return set_error(PP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 1024]");
+  if (t->block_threads < 64 || t->block_threads > 512 || (t->block_threads % 32) != 0)
+    return set_error(PP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 512]");
+  if (t->safety_cell < 0.0f) return set_error(PP_ERR_INVALID, "safety_cell must be >= 0");
   if (t->photons_per_thread < 1 || t->photons_per_thread > 4096)
     return set_error(PP_ERR_INVALID, "photons_per_thread must be in [1, 4096]");
   if (t->ctas_per_sm < 0) return set_error(PP_ERR_INVALID, "ctas_per_sm must be >= 0");
   DeviceScope ds(ctx->device);
   const bool ppt_changed = t->photons_per_thread != ctx->tuning.photons_per_thread;
-  const bool cell_changed = t->cell_size != ctx->tuning.cell_size;
+  const bool cell_changed =
+      t->cell_size != ctx->tuning.cell_size || t->safety_cell != ctx->tuning.safety_cell;
   ctx->tuning = *t;
   ctx->version++;
   if (ppt_changed && ctx->has_sources) {

@@ -132,6 +132,43 @@ __global__ void pack_kernel(const unsigned* __restrict__ counts, const unsigned*
   }
 }
 
+// One thread per safety cell: min over spheres of |c - s| - r - margin,
+// floored to the quantum.  Targets are staged through shared memory.
+__global__ void safety_kernel(const SafetyDev sg, const pp_sphere* __restrict__ t, int n,
+                              unsigned char* __restrict__ out) {
+  __shared__ float4 sh[256];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+  if (i < sg.n_cells) {
+    const int x = i % sg.dims[0];
+    const int y = (i / sg.dims[0]) % sg.dims[1];
+    const int z = i / (sg.dims[0] * sg.dims[1]);
+    cx = sg.lo[0] + (x + 0.5f) * sg.cell;
+    cy = sg.lo[1] + (y + 0.5f) * sg.cell;
+    cz = sg.lo[2] + (z + 0.5f) * sg.cell;
+  }
+  float best = 1e30f;
+  for (int base = 0; base < n; base += 256) {
+    const int j = base + threadIdx.x;
+    __syncthreads();
+    if (j < n)
+      sh[threadIdx.x] = make_float4(t[j].position[0], t[j].position[1], t[j].position[2],
+                                    t[j].radius + kGridMargin);
+    __syncthreads();
+    const int m = min(256, n - base);
+    for (int k = 0; k < m; ++k) {
+      const float4 s = sh[k];
+      const float dx = cx - s.x, dy = cy - s.y, dz = cz - s.z;
+      best = fminf(best, sqrtf(dx * dx + dy * dy + dz * dz) - s.w);
+    }
+  }
+  if (i < sg.n_cells) {
+    // 1 mm of slack covers the rounding of the distance itself
+    const float q = floorf((best - 1e-3f) / kSafetyQuantum);
+    out[i] = (unsigned char)fminf(fmaxf(q, 0.0f), 255.0f);
+  }
+}
+
 __global__ void hits_to_columns_kernel(const pp_hit_record* __restrict__ rec, long long n,
                                        pp_hits out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -307,6 +344,52 @@ int build_grid(const pp_sphere* targets_dev, int n, float cell_size, cudaStream_
   *grid_out = g;
   *blob_out = blob;
   *n_items_out = n_items;
+  return 0;
+}
+
+int build_safety(const pp_sphere* targets_dev, int n, const GridDev& grid, float cell,
+                 cudaStream_t stream, SafetyDev* out, unsigned char** field_out, std::string* err) {
+  *field_out = nullptr;
+  SafetyDev sg{};
+  double h = cell > 0.0f ? cell : 12.5;
+  double ext[3];
+  for (int a = 0; a < 3; ++a) ext[a] = (double)grid.hi[a] - (double)grid.lo[a];
+  for (int guard = 0; guard < 64; ++guard) {
+    double cells = 1.0;
+    for (int a = 0; a < 3; ++a) cells *= std::max(1.0, std::ceil(ext[a] / h));
+    if (cells <= 16.0 * 1024 * 1024) break;
+    h *= 1.25;
+  }
+  sg.n_cells = 1;
+  for (int a = 0; a < 3; ++a) {
+    sg.dims[a] = (int)std::max(1.0, std::ceil(ext[a] / h));
+    sg.lo[a] = grid.lo[a];
+    sg.hi[a] = (float)((double)grid.lo[a] + sg.dims[a] * h);
+    sg.n_cells *= sg.dims[a];
+  }
+  sg.cell = (float)h;
+  sg.inv_cell = (float)(1.0 / h);
+  sg.bytes = (uint32_t)(((size_t)sg.n_cells + 15) & ~(size_t)15);
+  unsigned char* f = nullptr;
+  if (cudaMalloc(&f, (size_t)sg.bytes) != cudaSuccess) {
+    if (err) *err = "cudaMalloc(safety field) failed";
+    return -1;
+  }
+  cudaMemsetAsync(f, 0, (size_t)sg.bytes, stream);
+  if (n <= 0) {
+    cudaMemsetAsync(f, 255, (size_t)sg.n_cells, stream);
+  } else {
+    safety_kernel<<<(sg.n_cells + 255) / 256, 256, 0, stream>>>(sg, targets_dev, n, f);
+  }
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaFree(f);
+    if (err) *err = std::string("safety field: ") + cudaGetErrorString(e);
+    return -1;
+  }
+  *out = sg;
+  *field_out = f;
   return 0;
 }
 

@@ -8,7 +8,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/pp_gb300.h"
+#include "pp_gb300.h"
 
 namespace pp {
 
@@ -29,6 +29,40 @@ struct GridDev {
   uint32_t off_items;    // byte offset of the item list in the blob
   uint32_t off_spheres;  // byte offset of the sphere table in the blob
   uint32_t blob_bytes;   // multiple of 16
+};
+
+// Safety field: a coarser-or-finer uniform grid over the same box whose cell
+// value is a lower bound on the distance from the cell centre to the nearest
+// (inflated) sphere surface, quantised down in kSafetyQuantum steps (uint8).
+// A step segment lies inside the ball of radius L/2 about its midpoint m; if
+// D(centre) - |m - centre| > L/2 (1-Lipschitz) no sphere can be hit.
+struct SafetyDev {
+  float lo[3];
+  float hi[3];
+  float cell;      // edge (m), cubic cells
+  float inv_cell;
+  int dims[3];
+  int n_cells;
+  uint32_t bytes;  // allocation, n_cells rounded up to 16 (padding bytes are 0)
+};
+constexpr float kSafetyQuantum = 0.5f;  // m per uint8 step (saturates at 127.5 m)
+
+// Per-warp shared-memory state of the propagation kernel: the queue of
+// deferred step segments and, per lane, the earliest hit found so far.
+constexpr int kQueueCap = 32;
+constexpr int kMaxBlockThreads = 512;
+struct WarpQueue {
+  float px[kQueueCap], py[kQueueCap], pz[kQueueCap];
+  float dx[kQueueCap], dy[kQueueCap], dz[kQueueCap];
+  float len[kQueueCap];
+  float dist0[kQueueCap];     // compensated path length at the segment start
+  uint32_t meta[kQueueCap];   // owner lane | step << 8
+};
+struct WarpBest {
+  uint32_t key[32];           // step << 16 | target index; ~0 = none
+  float hx[32], hy[32], hz[32];
+  float ox[32], oy[32], oz[32];
+  float dist[32];
 };
 
 constexpr uint32_t kCellStartBits = 20;                    // first item index
@@ -60,6 +94,8 @@ struct LaunchArgs {
 
   const unsigned char* blob;               // grid blob (global memory)
   GridDev grid;
+  const unsigned char* safety;             // safety field (global memory)
+  SafetyDev sgrid;
 
   const float4* medium;                    // {sca_len, v_group, abs_len, n}
   int n_medium;
@@ -80,22 +116,44 @@ struct LaunchArgs {
   unsigned long long capacity;
   pp_counters* counters;
   unsigned long long wait_limit_ns;        // bound on the TMA staging wait
+
+  uint32_t safety_offset;                  // shared-memory offset of the staged field
+  uint32_t state_offset;                   // shared-memory offset of the warp state
+  int warps_per_block;
 };
+
+// Dynamic shared memory of one CTA: [grid blob | safety field] when staged,
+// then the per-warp state.
+inline size_t propagate_smem_bytes(uint32_t blob_bytes, uint32_t safety_bytes, bool smem_tables,
+                                   int block_threads, uint32_t* safety_offset,
+                                   uint32_t* state_offset) {
+  const size_t blob = ((size_t)blob_bytes + 15) & ~(size_t)15;
+  const size_t field = ((size_t)safety_bytes + 15) & ~(size_t)15;
+  const size_t off = smem_tables ? blob + field : 0;
+  if (safety_offset) *safety_offset = (uint32_t)blob;
+  if (state_offset) *state_offset = (uint32_t)off;
+  return off + (size_t)(block_threads / 32) * (sizeof(WarpQueue) + sizeof(WarpBest));
+}
+// Largest dynamic shared memory per CTA for which two CTAs fit on an SM.
+constexpr size_t kSmemPerCtaBudget = 110 * 1024;
 
 // Host-side launch of the propagation kernel (pp_propagate.cu).
 cudaError_t launch_propagate(const LaunchArgs& args, int block_threads, int ctas_per_sm,
                              bool precise, bool smem_grid, int num_sms, cudaStream_t stream,
                              int* grid_out);
-// Maximum dynamic shared memory the kernel may use for the staged blob.
-size_t max_smem_blob_bytes();
 // Resident CTAs per SM for a configuration (occupancy calculator).
-int propagate_occupancy(int block_threads, bool precise, bool smem_grid, size_t smem_bytes);
+int propagate_occupancy(int block_threads, bool precise, bool smem_tables, uint32_t blob_bytes,
+                        uint32_t safety_bytes);
 
 // Grid build on the device (pp_grid.cu).  targets_dev: n spheres in device
 // memory.  Returns 0 on success; *blob_out is allocated with cudaMalloc.
 int build_grid(const pp_sphere* targets_dev, int n, float cell_size, cudaStream_t stream,
                GridDev* grid_out, unsigned char** blob_out, long long* n_items_out,
                std::string* err);
+
+// Safety field over the grid box (pp_grid.cu); *field_out is cudaMalloc'd.
+int build_safety(const pp_sphere* targets_dev, int n, const GridDev& grid, float cell,
+                 cudaStream_t stream, SafetyDev* out, unsigned char** field_out, std::string* err);
 
 // Scatter hit records into columns on the device (pp_grid.cu).
 cudaError_t launch_hits_to_columns(const pp_hit_record* rec, long long n, const pp_hits& out,

@@ -5,21 +5,30 @@
 // replay variant (IEEE math library, compiled with -fmad=false so that every
 // FP32 expression rounds exactly as the CPU oracle's does).
 //
-//
 // Replaces cuda_propagate_photons! (PhotonPropagation.jl v0.9.3,
 // src/photon_prop_cuda.jl:429-549) and its one-launch-per-source host loop
 // (:927-943).  Design:
-//   * persistent CTAs (a multiple of the SM count); every warp pulls chunks of
-//     32 * photons_per_thread photons of one source from a device work queue,
-//     so one launch covers any number of sources with uneven photon counts;
+//   * persistent CTAs; every warp pulls chunks of 32 * photons_per_thread
+//     photons of one source from a device work queue, so one launch covers any
+//     number of sources with uneven photon counts;
 //   * photon i of source s draws its random numbers from Philox4x32-10 at
-//     counter (i, call, s) and key = seed, so results do not depend on the
-//     launch shape and any photon range can be replayed;
-//   * the target culling grid (cells, candidate lists, spheres) is staged
-//     once per CTA into shared memory with a TMA bulk copy (cp.async.bulk)
-//     completing on an mbarrier, waited on with a time bound;
-//   * hits are appended with one atomic per warp (warp-aggregated) into an
-//     80-byte record written as five 16-byte vector stores.
+//     counter (i, call, s) and key = seed: results do not depend on the launch
+//     shape and any photon range can be replayed;
+//   * speculative stepping with deferred hit tests.  Each lane runs all
+//     n_steps of its photon without waiting for the target test.  A step
+//     segment is cleared cheaply when the safety field proves that no target
+//     lies within the ball around its midpoint (or the two balls around its
+//     quarter points); the rare uncleared segments go to a per-warp queue in
+//     shared memory that the warp drains densely, one segment per lane,
+//     through the uniform-grid DDA.  The photon's hit is the earliest step
+//     with an intersection and, within it, the lowest target index -- the
+//     reference's "first target in index order" (:497-506).  Steps after the
+//     hit were computed speculatively and are discarded;
+//   * the target grid (cells, candidate lists, spheres) is staged once per CTA
+//     into shared memory with a TMA bulk copy completing on an mbarrier, waited
+//     on with a time bound;
+//   * hits are appended with one atomic per warp into 80-byte records written
+//     as five 16-byte vector stores.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -46,11 +55,27 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Stage `bytes` (multiple of 16, 16-byte aligned source) into shared memory
-// with TMA bulk copies that complete on one mbarrier.  Every thread then waits
-// on the barrier's phase 0 for at most limit_ns.  Returns false on timeout.
-__device__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_t bytes,
-                           unsigned long long* bar, unsigned long long limit_ns) {
+// Issue TMA bulk copies of `bytes` (multiple of 16, both ends 16-byte
+// aligned) completing on the mbarrier at bar_a.
+__device__ __forceinline__ void bulk_copy(unsigned char* dst, const unsigned char* src,
+                                          uint32_t bytes, uint32_t bar_a) {
+  constexpr uint32_t kChunk = 32768;
+  for (uint32_t off = 0; off < bytes; off += kChunk) {
+    const uint32_t n = bytes - off < kChunk ? bytes - off : kChunk;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst + off)),
+        "l"(src + off), "r"(n), "r"(bar_a)
+        : "memory");
+  }
+}
+
+// Stage two global tables into shared memory with TMA bulk copies completing
+// on one mbarrier.  Every thread then waits on the barrier's phase 0 for at
+// most limit_ns.  Returns false on timeout.
+__device__ bool stage_tables(unsigned char* dst0, const unsigned char* src0, uint32_t bytes0,
+                             unsigned char* dst1, const unsigned char* src1, uint32_t bytes1,
+                             unsigned long long* bar, unsigned long long limit_ns) {
   const uint32_t bar_a = smem_addr(bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar_a), "r"(1) : "memory");
@@ -59,17 +84,11 @@ __device__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a), "r"(bytes)
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
+                 "r"(bytes0 + bytes1)
                  : "memory");
-    constexpr uint32_t kChunk = 32768;
-    for (uint32_t off = 0; off < bytes; off += kChunk) {
-      const uint32_t n = bytes - off < kChunk ? bytes - off : kChunk;
-      asm volatile(
-          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-              smem_addr(dst + off)),
-          "l"(src + off), "r"(n), "r"(bar_a)
-          : "memory");
-    }
+    bulk_copy(dst0, src0, bytes0, bar_a);
+    bulk_copy(dst1, src1, bytes1, bar_a);
   }
   const unsigned long long t0 = global_timer_ns();
   while (true) {
@@ -86,7 +105,83 @@ __device__ bool stage_blob(unsigned char* dst, const unsigned char* src, uint32_
   }
 }
 
-// Append one hit: one atomic per warp for all lanes that hit in this step.
+// True when the safety field proves that no (inflated) target sphere meets
+// the ball of radius R about m.  Branch-free: two lower bounds on the distance
+// from m to every target, of which the larger must exceed R --
+//   the distance from m to the field's box (which contains every target), and
+//   D(c) - |m - c| for the centre c of the field cell nearest to m (distance
+//   to the targets is 1-Lipschitz; D(c) is stored quantised down).
+template <bool kShared>
+__device__ __forceinline__ bool ball_clear(const SafetyDev& s, const unsigned char* __restrict__ f,
+                                           float3 m, float R) {
+  const float dx = fmaxf(fmaxf(s.lo[0] - m.x, m.x - s.hi[0]), 0.0f);
+  const float dy = fmaxf(fmaxf(s.lo[1] - m.y, m.y - s.hi[1]), 0.0f);
+  const float dz = fmaxf(fmaxf(s.lo[2] - m.z, m.z - s.hi[2]), 0.0f);
+  const float box2 = dx * dx + dy * dy + dz * dz;
+  const float fx = fminf(fmaxf(floorf((m.x - s.lo[0]) * s.inv_cell), 0.0f), (float)(s.dims[0] - 1));
+  const float fy = fminf(fmaxf(floorf((m.y - s.lo[1]) * s.inv_cell), 0.0f), (float)(s.dims[1] - 1));
+  const float fz = fminf(fmaxf(floorf((m.z - s.lo[2]) * s.inv_cell), 0.0f), (float)(s.dims[2] - 1));
+  const int idx = (int)fmaf(fmaf(fz, (float)s.dims[1], fy), (float)s.dims[0], fx);
+  const float D = (float)(kShared ? f[idx] : __ldg(f + idx)) * kSafetyQuantum;
+  const float ox = fmaf(fx + 0.5f, s.cell, s.lo[0]) - m.x;
+  const float oy = fmaf(fy + 0.5f, s.cell, s.lo[1]) - m.y;
+  const float oz = fmaf(fz + 0.5f, s.cell, s.lo[2]) - m.z;
+  const float budget = D - R;
+  return box2 > R * R || (budget > 0.0f && ox * ox + oy * oy + oz * oz < budget * budget);
+}
+
+// The segment pos + t*dir, t in [0, L], provably misses every target: it lies
+// inside the ball of radius L/2 about its midpoint.
+template <bool kShared>
+__device__ __forceinline__ bool segment_clear(const SafetyDev& s, const unsigned char* f,
+                                              float3 pos, float3 dir, float L) {
+  const float h = 0.5f * L;
+  return ball_clear<kShared>(
+      s, f, make_float3(fmaf(dir.x, h, pos.x), fmaf(dir.y, h, pos.y), fmaf(dir.z, h, pos.z)),
+      h * 1.0001f + 1e-4f);
+}
+
+// Drain the warp's deferred segments: lane e tests queue entry base + e with
+// the grid DDA; the earliest (step, target) per owner lane wins via a shared
+// atomicMin on the key (step << 16 | target), and the winning lane writes
+// the hit state into the owner's slot.
+template <bool P>
+__device__ __forceinline__ void drain_queue(WarpQueue& q, WarpBest& b, int count,
+                                            const GridDev& g, const uint32_t* cells,
+                                            const uint16_t* items, const float4* sph, int lane) {
+  for (int base = 0; base < count; base += 32) {
+    const int e = base + lane;
+    int j = -1, owner = 0;
+    uint32_t key = 0;
+    float d = 0.0f, d0 = 0.0f;
+    float3 p = make_float3(0.0f, 0.0f, 0.0f), dir = p;
+    if (e < count) {
+      p = make_float3(q.px[e], q.py[e], q.pz[e]);
+      dir = make_float3(q.dx[e], q.dy[e], q.dz[e]);
+      d0 = q.dist0[e];
+      const uint32_t meta = q.meta[e];
+      owner = (int)(meta & 31u);
+      j = first_hit<P>(g, cells, items, sph, p, dir, q.len[e], &d);
+      if (j >= 0) {
+        key = ((meta >> 8) << 16) | (uint32_t)j;
+        atomicMin(&b.key[owner], key);
+      }
+    }
+    __syncwarp();
+    if (j >= 0 && b.key[owner] == key) {
+      b.hx[owner] = madd<P>(dir.x, d, p.x);
+      b.hy[owner] = madd<P>(dir.y, d, p.y);
+      b.hz[owner] = madd<P>(dir.z, d, p.z);
+      b.ox[owner] = dir.x;
+      b.oy[owner] = dir.y;
+      b.oz[owner] = dir.z;
+      b.dist[owner] = d0 + d;
+    }
+    __syncwarp();
+  }
+}
+
+// Append one hit: one atomic per warp for all lanes that record in this pass.
 __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, float wl, float3 dir,
                                            float dist, float3 idir, float abs_w, double time,
                                            long long photon, int module_index, int n_steps,
@@ -101,11 +196,10 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
   const unsigned long long slot = base + rank;
   if (slot < a.capacity) {
     float4* r = reinterpret_cast<float4*>(a.hits + slot);
-    const double2 tp = make_double2(time, __longlong_as_double(photon));
     r[0] = make_float4(pos.x, pos.y, pos.z, wl);
     r[1] = make_float4(dir.x, dir.y, dir.z, dist);
     r[2] = make_float4(idir.x, idir.y, idir.z, abs_w);
-    reinterpret_cast<double2*>(r)[3] = tp;
+    reinterpret_cast<double2*>(r)[3] = make_double2(time, __longlong_as_double(photon));
     r[4] = make_float4(__int_as_float(module_index), __int_as_float(n_steps),
                        __int_as_float(source_index), 0.0f);
   } else {
@@ -114,30 +208,44 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
   }
 }
 
+// Two CTAs of kMaxBlockThreads per SM caps the kernel at 64 registers.
+#ifndef PP_PROPAGATE_MIN_BLOCKS
+#define PP_PROPAGATE_MIN_BLOCKS 2
+#endif
+
 template <bool kPrecise, bool kSmemGrid>
-__global__ void propagate_kernel(const __grid_constant__ LaunchArgs a) {
+__global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
+    propagate_kernel(const __grid_constant__ LaunchArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar;
 
   const uint32_t* cells;
   const uint16_t* items;
   const float4* sph;
+  const unsigned char* field;
   if (kSmemGrid) {
-    if (!stage_blob(smem, a.blob, a.grid.blob_bytes, &bar, a.wait_limit_ns)) {
+    if (!stage_tables(smem, a.blob, a.grid.blob_bytes, smem + a.safety_offset, a.safety,
+                      a.sgrid.bytes, &bar, a.wait_limit_ns)) {
       atomicOr(&a.counters->err_flags, (unsigned)PP_FLAG_TIMEOUT);
       return;
     }
     cells = reinterpret_cast<const uint32_t*>(smem);
     items = reinterpret_cast<const uint16_t*>(smem + a.grid.off_items);
     sph = reinterpret_cast<const float4*>(smem + a.grid.off_spheres);
+    field = smem + a.safety_offset;
   } else {
     cells = reinterpret_cast<const uint32_t*>(a.blob);
     items = reinterpret_cast<const uint16_t*>(a.blob + a.grid.off_items);
     sph = reinterpret_cast<const float4*>(a.blob + a.grid.off_spheres);
+    field = a.safety;
   }
   const bool have_grid = a.grid.n_targets > 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  WarpQueue& q = reinterpret_cast<WarpQueue*>(smem + a.state_offset)[warp];
+  WarpBest& best = reinterpret_cast<WarpBest*>(smem + a.state_offset +
+                                               a.warps_per_block * sizeof(WarpQueue))[warp];
+  const unsigned lanemask_lt = (1u << lane) - 1u;
 
-  const int lane = threadIdx.x & 31;
   unsigned long long steps_acc = 0, sim_acc = 0;
 
   while (true) {
@@ -169,8 +277,10 @@ __global__ void propagate_kernel(const __grid_constant__ LaunchArgs a) {
     const float stime = __ldg(&sp->time);
     const long long first = __ldg(&sp->first_photon);
 
-    for (long long pl = p0 + lane; pl < pend; pl += 32) {
-      const long long p = first + pl;  // global photon index (RNG counter)
+    for (long long base = p0; base < pend; base += 32) {
+      const bool active = base + lane < pend;
+      // Lanes past the end replay the first photon of the round (never recorded).
+      const long long p = first + (active ? base + lane : base);
       const uint32_t plo = (uint32_t)p, phi = (uint32_t)((unsigned long long)p >> 32);
       const uint4 r0 = philox(make_uint4(plo, phi, 0u, (uint32_t)s), a.key0, a.key1);
       const float u0 = u01(r0.x), u1 = u01(r0.y), u2 = u01(r0.z), u3 = u01(r0.w);
@@ -246,28 +356,34 @@ __global__ void propagate_kernel(const __grid_constant__ LaunchArgs a) {
       const float3 idir = dir;
       const float sca_len = med.x;
       float dist = 0.0f, comp = 0.0f;  // Kahan-compensated path length
-      bool overflowed = false;
-      int k = 1;
-      for (; k <= a.n_steps; ++k) {
+      best.key[lane] = 0xffffffffu;
+      __syncwarp();
+      int count = 0;  // warp-uniform length of the deferred-segment queue
+      for (int k = 1; k <= a.n_steps; ++k) {
         const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.key0, a.key1);
         const float step = -f_log<kPrecise>(u01(r.x)) * sca_len;
-        float d = 0.0f;
-        const int j = have_grid ? first_hit<kPrecise>(a.grid, cells, items, sph, pos, dir, step, &d)
-                                : -1;
-        if (j >= 0) {
-          pos = make_float3(madd<kPrecise>(dir.x, d, pos.x), madd<kPrecise>(dir.y, d, pos.y),
-                            madd<kPrecise>(dir.z, d, pos.z));
-          {
-            const float y = d - comp, t = dist + y;
-            comp = (t - dist) - y;
-            dist = t;
+        const bool need = have_grid && active && !segment_clear<kSmemGrid>(a.sgrid, field, pos, dir, step);
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        if (m) {
+          const int nn = __popc(m);
+          if (count + nn > kQueueCap) {
+            drain_queue<kPrecise>(q, best, count, a.grid, cells, items, sph, lane);
+            count = 0;
           }
-          const double dist_c = (double)dist - (double)comp;
-          const double time = (double)t0 + dist_c / (double)med.y;
-          const float dist_f = (float)dist_c;
-          const float abs_w = f_exp<kPrecise>(-f_div<kPrecise>(dist_f, med.z));
-          record_hit(a, pos, wl, dir, dist_f, idir, abs_w, time, p, j + 1, k, s, &overflowed);
-          break;
+          if (need) {
+            const int e = count + __popc(m & lanemask_lt);
+            q.px[e] = pos.x;
+            q.py[e] = pos.y;
+            q.pz[e] = pos.z;
+            q.dx[e] = dir.x;
+            q.dy[e] = dir.y;
+            q.dz[e] = dir.z;
+            q.len[e] = step;
+            q.dist0[e] = dist - comp;
+            q.meta[e] = (uint32_t)lane | ((uint32_t)k << 8);
+          }
+          count += nn;
+          __syncwarp();
         }
         pos = make_float3(madd<kPrecise>(dir.x, step, pos.x), madd<kPrecise>(dir.y, step, pos.y),
                           madd<kPrecise>(dir.z, step, pos.z));
@@ -278,8 +394,26 @@ __global__ void propagate_kernel(const __grid_constant__ LaunchArgs a) {
         }
         dir = update_direction<kPrecise>(a.phase, dir, u01(r.y), u01(r.z), u01(r.w));
       }
-      steps_acc += (unsigned long long)min(k, a.n_steps);
-      if (!overflowed) sim_acc += 1;
+      if (count > 0) drain_queue<kPrecise>(q, best, count, a.grid, cells, items, sph, lane);
+      __syncwarp();
+
+      const uint32_t key = best.key[lane];
+      bool overflowed = false;
+      int steps_taken = a.n_steps;
+      if (active && key != 0xffffffffu) {
+        steps_taken = (int)(key >> 16);
+        const float3 hpos = make_float3(best.hx[lane], best.hy[lane], best.hz[lane]);
+        const float3 hdir = make_float3(best.ox[lane], best.oy[lane], best.oz[lane]);
+        const float hdist = best.dist[lane];
+        const double time = (double)t0 + (double)hdist / (double)med.y;
+        const float abs_w = f_exp<kPrecise>(-f_div<kPrecise>(hdist, med.z));
+        record_hit(a, hpos, wl, hdir, hdist, idir, abs_w, time, p, (int)(key & 0xffffu) + 1,
+                   steps_taken, s, &overflowed);
+      }
+      if (active) {
+        steps_acc += (unsigned long long)steps_taken;
+        if (!overflowed) sim_acc += 1;
+      }
     }
   }
 

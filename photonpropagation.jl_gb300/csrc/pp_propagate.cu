@@ -19,10 +19,11 @@ const void* select_kernel(bool precise, bool smem_grid) {
 
 }  // namespace
 
-size_t max_smem_blob_bytes() { return 200 * 1024; }
-
-int propagate_occupancy(int block_threads, bool precise, bool smem_grid, size_t smem_bytes) {
-  const void* k = select_kernel(precise, smem_grid);
+int propagate_occupancy(int block_threads, bool precise, bool smem_tables, uint32_t blob_bytes,
+                        uint32_t safety_bytes) {
+  const void* k = select_kernel(precise, smem_tables);
+  const size_t smem_bytes = propagate_smem_bytes(blob_bytes, safety_bytes, smem_tables,
+                                                 block_threads, nullptr, nullptr);
   if (smem_bytes > 48 * 1024)
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
   int n = 0;
@@ -35,7 +36,11 @@ cudaError_t launch_propagate(const LaunchArgs& args, int block_threads, int ctas
                              bool precise, bool smem_grid, int num_sms, cudaStream_t stream,
                              int* grid_out) {
   const void* k = select_kernel(precise, smem_grid);
-  const size_t smem = smem_grid ? args.grid.blob_bytes : 0;
+  if (block_threads > kMaxBlockThreads || block_threads % 32) return cudaErrorInvalidValue;
+  LaunchArgs a = args;
+  const size_t smem = propagate_smem_bytes(args.grid.blob_bytes, args.sgrid.bytes, smem_grid,
+                                           block_threads, &a.safety_offset, &a.state_offset);
+  a.warps_per_block = block_threads / 32;
   cudaError_t e;
   if (smem > 48 * 1024) {
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -52,7 +57,7 @@ cudaError_t launch_propagate(const LaunchArgs& args, int block_threads, int ctas
   const unsigned long long need = (args.total_chunks + warps_per_cta - 1) / warps_per_cta;
   if (need < (unsigned long long)grid) grid = (int)(need > 0 ? need : 1);
   if (grid_out) *grid_out = grid;
-  void* params[] = {const_cast<LaunchArgs*>(&args)};
+  void* params[] = {&a};
   return cudaLaunchKernel(k, dim3(grid), dim3(block_threads), params, smem, stream);
 }
 

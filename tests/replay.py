@@ -77,7 +77,8 @@ def _compare(got, want, spheres_xyzr, rel, grazing_cos, min_match, max_nongrazin
                          round(float(np.asarray(t["dist_travelled"])[i]), 3)))
     assert nongrazing <= max(1, max_nongrazing * total), (
         f"{nongrazing} non-grazing one-sided hits of {total}: {diag}")
-    assert len(common) >= min_match * total, (len(common), total, diag)
+    grazing = len(only_g) + len(only_w) - nongrazing
+    assert len(common) + grazing >= min_match * total, (len(common), total, diag)
 
     g = {k: np.asarray(v)[ig] for k, v in got.items() if hasattr(v, "__len__")}
     w = {k: np.asarray(v)[iw] for k, v in want.items() if hasattr(v, "__len__")}
