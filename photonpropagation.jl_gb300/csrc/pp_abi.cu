@@ -139,7 +139,7 @@ struct pp_ctx {
   bool has_sources = false;
   bool needs_track = false;
 
-  pp_tuning tuning{256, 8, 0, 0, 0.0f, 0, 0.0f, 0};
+  pp_tuning tuning{512, 8, 0, 0, 0.0f, 0, 0.0f, 0};
 
   // scratch of pp_propagate
   pp_hit_record* d_hits = nullptr;
@@ -799,21 +799,20 @@ PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sampl
     return PP_OK;
   };
 
-  // Stage 1: cell size at the current launch shape.  Stage 2: launch shape at
-  // the best cell size.
-  float auto_h = ctx->grid.cell[0];
-  if (ctx->tuning.cell_size <= 0.0f) {
-    // recover the automatic size
-    auto_h = ctx->grid.cell[0];
-  }
+  // Stage 1: grid cell size, then stage 2: safety-field cell size, both at a
+  // 512-thread launch; stage 3: launch shape at the chosen sizes.
+  const float auto_h = ctx->grid.cell[0];
+  const float auto_s = ctx->sgrid.cell;
   pp_tuning best = orig_tuning;
+  best.block_threads = 512;
   double best_ms = 1e300;
-  const float cell_factors[] = {0.5f, 0.75f, 1.0f, 1.5f, 2.0f, 3.0f};
-  float best_h = ctx->grid.cell[0];
   if (!ctx->h_targets.empty()) {
+    const float cell_factors[] = {0.75f, 1.0f, 1.5f, 2.0f};
+    float best_h = auto_h;
     for (float cf : cell_factors) {
       pp_tuning t = best;
       t.cell_size = auto_h * cf;
+      ctx->tuning.safety_cell = auto_s;
       if (rebuild_grid(ctx, t.cell_size) != PP_OK) continue;
       double ms;
       if (time_config(t, &ms) != PP_OK) continue;
@@ -823,6 +822,23 @@ PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sampl
       }
     }
     best.cell_size = best_h;
+    best_ms = 1e300;
+    const float safety_factors[] = {1.0f, 0.6f};
+    float best_s = auto_s;
+    for (float sf : safety_factors) {
+      pp_tuning t = best;
+      t.safety_cell = auto_s * sf;
+      ctx->tuning.safety_cell = t.safety_cell;
+      if (rebuild_grid(ctx, best_h) != PP_OK) continue;
+      double ms;
+      if (time_config(t, &ms) != PP_OK) continue;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_s = t.safety_cell;
+      }
+    }
+    best.safety_cell = best_s;
+    ctx->tuning.safety_cell = best_s;
     if (rebuild_grid(ctx, best_h) != PP_OK) {
       ctx->tuning = orig_tuning;
       finish(0);
@@ -831,8 +847,8 @@ PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sampl
     }
   }
   best_ms = 1e300;
-  const int blocks[] = {128, 256, 512};
-  const int ppts[] = {1, 2, 4, 8, 16};
+  const int blocks[] = {256, 512};
+  const int ppts[] = {2, 8};
   for (int b : blocks) {
     for (int p : ppts) {
       pp_tuning t = best;
