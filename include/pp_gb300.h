@@ -271,6 +271,32 @@ PP_API int pp_fetch_hits(pp_ctx* ctx, const pp_hits* out, int64_t n);
  * make_hit_buffers, src/photon_prop_cuda.jl:878-880). */
 PP_API int pp_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
 
+/* Size of the device array that pp_propagate_static takes its scratch from. */
+#define PP_STATIC_SCRATCH_BYTES (8u * 1024u * 1024u)
+
+/* Propagation that allocates no device memory.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc -- code running
+ * while another framework's pooling allocator owns the device memory, code
+ * recorded into a CUDA graph by its caller, services that fix their memory
+ * use at start-up.  Inputs are host arrays (medium tables, spectrum knots or
+ * a monochromatic wavelength, track table, targets, sources); hits go to the
+ * caller's device buffer d_hits (16-byte aligned, `capacity` records) and the
+ * launch's counters to the host struct *counters.  All scratch (device copies
+ * of the inputs, culling grid, safety field, work queue, counters) comes from
+ * one static device array of PP_STATIC_SCRATCH_BYTES (8 MiB), which every GPU
+ * that loads this library holds until exit; inputs needing more are rejected
+ * with PP_ERR_INVALID.  The first call on a device looks up the array's
+ * address: make it before any stream capture.  Calls share the array, so calls
+ * that overlap on the GPU race.  Runs on the current device, synchronously on
+ * `stream`; returns PP_ERR_OVERFLOW when more than `capacity` hits occur. */
+PP_API int pp_propagate_static(const pp_medium* medium, const float* spectrum_knots,
+                               int32_t n_spectrum, float mono_wavelength,
+                               const float* track_quantiles, int32_t n_track,
+                               const pp_sphere* targets, int32_t n_targets, float cell_size,
+                               const pp_source* sources, int32_t n_src, int64_t seed,
+                               int32_t n_steps, float photon_scaling, pp_hit_record* d_hits,
+                               int64_t capacity, pp_counters* counters, void* stream);
+
 /* Scatter n device hit records into device columns (structure of arrays). */
 PP_API int pp_hits_to_columns(const pp_hit_record* d_records, int64_t n, const pp_hits* d_out,
                               void* stream);

@@ -140,6 +140,11 @@ SIGNATURES = {
                                POINTER(pp_hits), c_int64, POINTER(c_int64), POINTER(c_int64)]),
     "pp_fetch_hits": (c_int32, [c_void_p, POINTER(pp_hits), c_int64]),
     "pp_device_memory": (c_int32, [c_int32, POINTER(c_int64), POINTER(c_int64)]),
+    "pp_propagate_static": (c_int32, [POINTER(pp_medium), POINTER(c_float), c_int32, c_float,
+                                      POINTER(c_float), c_int32, POINTER(pp_sphere), c_int32,
+                                      c_float, POINTER(pp_source), c_int32, c_int64, c_int32,
+                                      c_float, c_void_p, c_int64, POINTER(pp_counters),
+                                      c_void_p]),
     "pp_hits_to_columns": (c_int32, [c_void_p, c_int64, POINTER(pp_hits), c_void_p]),
     "pp_autotune": (c_int32, [c_void_p, c_int64, c_int32, c_int64, POINTER(pp_tuning),
                               POINTER(c_double)]),

@@ -79,6 +79,14 @@ bool kind_uses_track(int kind) {
 
 }  // namespace
 
+namespace pp {
+// Error reporting for entry points defined in other translation units.
+int report_error(int code, const std::string& message) {
+  g_last_error = message;
+  return code;
+}
+}  // namespace pp
+
 struct GraphKey {
   long long seed = 0;
   int n_steps = 0;

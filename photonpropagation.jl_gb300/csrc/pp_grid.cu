@@ -393,6 +393,68 @@ int build_safety(const pp_sphere* targets_dev, int n, const GridDev& grid, float
   return 0;
 }
 
+int build_grid_into(const pp_sphere* targets_dev, int n, const GridDev& shape, unsigned* d_counts,
+                    unsigned* d_start, unsigned* d_cursor, unsigned* d_totals,
+                    unsigned char* d_blob, size_t blob_capacity, cudaStream_t stream,
+                    GridDev* grid_out, long long* n_items_out, std::string* err) {
+  auto fail = [&](const std::string& m) {
+    if (err) *err = m;
+    return -1;
+  };
+  GridDev g = shape;
+  const size_t cbytes = (size_t)g.n_cells * sizeof(unsigned);
+  cudaMemsetAsync(d_counts, 0, cbytes, stream);
+  cudaMemsetAsync(d_cursor, 0, cbytes, stream);
+  const int tb = 256;
+  if (n > 0) count_kernel<<<(n + tb - 1) / tb, tb, 0, stream>>>(g, targets_dev, n, d_counts);
+  scan_kernel<<<1, 1024, 0, stream>>>(d_counts, g.n_cells, d_start, d_totals);
+  unsigned tot[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(tot, d_totals, sizeof(tot), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return fail(std::string("grid count: ") + cudaGetErrorString(e));
+  const long long n_items = tot[0];
+  if (n_items > (long long)kCellStartMask || tot[1] > kCellMaxCount)
+    return fail("grid too dense: choose a smaller cell size");
+  auto pad16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  const size_t cells_b = pad16(cbytes);
+  const size_t items_b = pad16((size_t)std::max<long long>(n_items, 1) * sizeof(uint16_t));
+  const size_t total = cells_b + items_b + (size_t)n * sizeof(float4);
+  if (total > blob_capacity) return fail("grid larger than the space reserved for it");
+  g.off_items = (uint32_t)cells_b;
+  g.off_spheres = (uint32_t)(cells_b + items_b);
+  g.blob_bytes = (uint32_t)total;
+  g.n_targets = n;
+  cudaMemsetAsync(d_blob, 0, total, stream);
+  if (n > 0)
+    fill_kernel<<<(n + tb - 1) / tb, tb, 0, stream>>>(g, targets_dev, n, d_start, d_cursor,
+                                                     reinterpret_cast<uint16_t*>(d_blob + g.off_items));
+  const int m = std::max(g.n_cells, n);
+  pack_kernel<<<(m + tb - 1) / tb, tb, 0, stream>>>(
+      d_counts, d_start, g.n_cells, reinterpret_cast<uint32_t*>(d_blob), targets_dev, n,
+      reinterpret_cast<float4*>(d_blob + g.off_spheres));
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(std::string("grid build: ") + cudaGetErrorString(e));
+  *grid_out = g;
+  *n_items_out = n_items;
+  return 0;
+}
+
+int build_safety_into(const pp_sphere* targets_dev, int n, const SafetyDev& shape,
+                      unsigned char* d_field, cudaStream_t stream, std::string* err) {
+  cudaMemsetAsync(d_field, 0, (size_t)shape.bytes, stream);
+  if (n <= 0) {
+    cudaMemsetAsync(d_field, 255, (size_t)shape.n_cells, stream);
+  } else {
+    safety_kernel<<<(shape.n_cells + 255) / 256, 256, 0, stream>>>(shape, targets_dev, n, d_field);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("safety field: ") + cudaGetErrorString(e);
+    return -1;
+  }
+  return 0;
+}
+
 cudaError_t launch_hits_to_columns(const pp_hit_record* rec, long long n, const pp_hits& out,
                                    cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;

@@ -151,6 +151,20 @@ int build_grid(const pp_sphere* targets_dev, int n, float cell_size, cudaStream_
                GridDev* grid_out, unsigned char** blob_out, long long* n_items_out,
                std::string* err);
 
+// Set the calling thread's last error (pp_abi.cu); returns code.
+int report_error(int code, const std::string& message);
+
+// Grid build into caller-provided device memory (pp_grid.cu): `shape` holds
+// the box, cell sizes and dims; d_counts/d_start/d_cursor have n_cells entries,
+// d_totals two.  Used by the entry point that allocates nothing.
+int build_grid_into(const pp_sphere* targets_dev, int n, const GridDev& shape, unsigned* d_counts,
+                    unsigned* d_start, unsigned* d_cursor, unsigned* d_totals,
+                    unsigned char* d_blob, size_t blob_capacity, cudaStream_t stream,
+                    GridDev* grid_out, long long* n_items_out, std::string* err);
+// Safety field into caller-provided device memory of shape.bytes bytes.
+int build_safety_into(const pp_sphere* targets_dev, int n, const SafetyDev& shape,
+                      unsigned char* d_field, cudaStream_t stream, std::string* err);
+
 // Safety field over the grid box (pp_grid.cu); *field_out is cudaMalloc'd.
 int build_safety(const pp_sphere* targets_dev, int n, const GridDev& grid, float cell,
                  cudaStream_t stream, SafetyDev* out, unsigned char** field_out, std::string* err);
