@@ -243,6 +243,19 @@ PP_API int pp_total_photons(const pp_ctx* ctx, int64_t* total);
 PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
                      int64_t capacity, pp_counters* d_counters, void* stream);
 
+/* Histogram form of pp_launch for photon-table generation: no hit records;
+ * every hit of source s adds its absorption weight to d_hist[s*(n_bins+1)]
+ * (expected hits) and to bin 1 + b, b the bin of
+ * log10(t - d_tgeo[s] + t_offset) on n_bins uniform bins over [log_lo, log_hi)
+ * (clamped into the edge bins).  d_tgeo: per-source geometric time (ns),
+ * device memory.  Replaces the hit-table -> per-PMT counts -> residual-time
+ * histogram pipeline of the reference's table scripts
+ * (scripts/photon_tables/photon_tables_photons.jl:33-151,
+ * src/calc.jl calc_time_residual!). */
+PP_API int pp_launch_histogram(pp_ctx* ctx, int64_t seed, int32_t n_steps, const float* d_tgeo,
+                               float* d_hist, int32_t n_bins, float t_offset, float log_lo,
+                               float log_hi, pp_counters* d_counters, void* stream);
+
 /* Same work as pp_launch, replayed from a CUDA graph (memset + kernel)
  * captured on first use for these arguments. */
 PP_API int pp_launch_graph(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
@@ -307,6 +320,40 @@ PP_API int pp_hits_to_columns(const pp_hit_record* d_records, int64_t n, const p
  * src/photon_prop_cuda.jl:914-921). */
 PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sample_photons,
                        pp_tuning* best, double* best_photons_per_s);
+
+/* ---- learned surrogate (no reference counterpart: the reference evaluates an
+ *      external PhotonSurrogateModel, examples/validation.jl:455,673-676) ---- */
+
+/* A small MLP (n_in -> n_layers x hidden SiLU -> 1 + n_bins) mapping
+ * source-module geometry to log expected hits and arrival-time logits,
+ * trained with BF16 tcgen05 kernels (FP32 accumulate, Poisson + multinomial
+ * NLL, Adam).  Parameters are packed FP32: for each layer W (rows x cols,
+ * padded, row-major) then b (rows), see pp_mlp_layout. */
+typedef struct pp_mlp pp_mlp;
+PP_API int pp_mlp_create(pp_mlp** out, int32_t device, int32_t n_in, int32_t hidden,
+                         int32_t n_layers, int32_t n_bins, int32_t max_batch, uint64_t seed);
+PP_API int pp_mlp_destroy(pp_mlp* mlp);
+PP_API int pp_mlp_num_params(const pp_mlp* mlp, int64_t* n);
+PP_API int pp_mlp_layout(const pp_mlp* mlp, int32_t layer, int64_t* off_w, int64_t* off_b,
+                         int32_t* rows, int32_t* cols);
+PP_API int pp_mlp_get_params(const pp_mlp* mlp, float* host, int64_t n);
+PP_API int pp_mlp_set_params(pp_mlp* mlp, const float* host, int64_t n);
+/* Training-graph forward: d_x (B x n_in, FP32, device) -> d_out (B x padded
+ * outputs, FP32, device): column 0 log expected count, 1..n_bins time logits. */
+PP_API int pp_mlp_forward(pp_mlp* mlp, const float* d_x, int32_t B, float* d_out, void* stream);
+/* Loss and parameter gradients (no update); host outputs may be NULL. */
+PP_API int pp_mlp_loss_grad(pp_mlp* mlp, const float* d_x, const float* d_count,
+                            const float* d_hist, int32_t B, float* host_grad, float* host_loss,
+                            void* stream);
+/* One Adam step (forward, backward, update), asynchronous on `stream`. */
+PP_API int pp_mlp_train_step(pp_mlp* mlp, const float* d_x, const float* d_count,
+                             const float* d_hist, int32_t B, float lr, void* stream);
+PP_API int pp_mlp_last_loss(pp_mlp* mlp, float* host_loss);
+/* One tcgen05 GEMM (test hook): C = A * B^T, BF16 in, FP32 out (k_split > 0:
+ * C += over K slices). */
+PP_API int pp_mlp_gemm_test(const void* d_a, int64_t lda, int32_t a_trans, const void* d_b,
+                            int64_t ldb, int32_t b_trans, int32_t M, int32_t N, int32_t K,
+                            int32_t k_split, float* d_c, int64_t ldc, void* stream);
 
 /* ---- diagnostics (no reference counterpart) -------------------------------- */
 

@@ -21,6 +21,6 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
 from .targets import HomogeneousDetector, Spherical
-from . import workloads
+from . import surrogate, workloads
 
 __all__ = [n for n in dir() if not n.startswith("_")]

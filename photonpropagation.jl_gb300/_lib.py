@@ -136,6 +136,8 @@ SIGNATURES = {
     "pp_launch": (c_int32, [c_void_p, c_int64, c_int32, c_void_p, c_int64, c_void_p, c_void_p]),
     "pp_launch_graph": (c_int32, [c_void_p, c_int64, c_int32, c_void_p, c_int64, c_void_p,
                                   c_void_p]),
+    "pp_launch_histogram": (c_int32, [c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_int32,
+                                      c_float, c_float, c_float, c_void_p, c_void_p]),
     "pp_propagate": (c_int32, [c_void_p, POINTER(pp_source), c_int32, c_int64, c_int32, c_float,
                                POINTER(pp_hits), c_int64, POINTER(c_int64), POINTER(c_int64)]),
     "pp_fetch_hits": (c_int32, [c_void_p, POINTER(pp_hits), c_int64]),
@@ -146,6 +148,23 @@ SIGNATURES = {
                                       c_float, c_void_p, c_int64, POINTER(pp_counters),
                                       c_void_p]),
     "pp_hits_to_columns": (c_int32, [c_void_p, c_int64, POINTER(pp_hits), c_void_p]),
+    "pp_mlp_create": (c_int32, [POINTER(c_void_p), c_int32, c_int32, c_int32, c_int32, c_int32,
+                                c_int32, c_uint64]),
+    "pp_mlp_destroy": (c_int32, [c_void_p]),
+    "pp_mlp_num_params": (c_int32, [c_void_p, POINTER(c_int64)]),
+    "pp_mlp_layout": (c_int32, [c_void_p, c_int32, POINTER(c_int64), POINTER(c_int64),
+                                POINTER(c_int32), POINTER(c_int32)]),
+    "pp_mlp_get_params": (c_int32, [c_void_p, POINTER(c_float), c_int64]),
+    "pp_mlp_set_params": (c_int32, [c_void_p, POINTER(c_float), c_int64]),
+    "pp_mlp_forward": (c_int32, [c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
+    "pp_mlp_loss_grad": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
+                                   POINTER(c_float), POINTER(c_float), c_void_p]),
+    "pp_mlp_train_step": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_float,
+                                    c_void_p]),
+    "pp_mlp_last_loss": (c_int32, [c_void_p, POINTER(c_float)]),
+    "pp_mlp_gemm_test": (c_int32, [c_void_p, c_int64, c_int32, c_void_p, c_int64, c_int32,
+                                   c_int32, c_int32, c_int32, c_int32, c_void_p, c_int64,
+                                   c_void_p]),
     "pp_autotune": (c_int32, [c_void_p, c_int64, c_int32, c_int64, POINTER(pp_tuning),
                               POINTER(c_double)]),
     "pp_debug_philox": (c_int32, [POINTER(c_uint32), c_int32, c_uint32, c_uint32,

@@ -572,6 +572,33 @@ PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* 
   return enqueue(ctx, seed, n_steps, d_hits, capacity, d_counters, (cudaStream_t)stream);
 }
 
+PP_API int pp_launch_histogram(pp_ctx* ctx, int64_t seed, int32_t n_steps, const float* d_tgeo,
+                               float* d_hist, int32_t n_bins, float t_offset, float log_lo,
+                               float log_hi, pp_counters* d_counters, void* stream) {
+  int rc = validate_launch(ctx, n_steps, nullptr, 0, d_counters);
+  if (rc != PP_OK) return rc;
+  if (!d_tgeo || !d_hist || n_bins < 1 || !(log_hi > log_lo))
+    return set_error(PP_ERR_INVALID, "histogram needs tgeo, hist, n_bins >= 1, log_hi > log_lo");
+  DeviceScope ds(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  PP_CUDA(cudaMemsetAsync(d_counters, 0, sizeof(pp_counters), s), "zero counters");
+  PP_CUDA(cudaMemsetAsync(d_hist, 0, sizeof(float) * (size_t)ctx->n_src * (n_bins + 1), s),
+          "zero histograms");
+  if (ctx->total_chunks == 0) return PP_OK;
+  LaunchArgs a = make_args(ctx, seed, n_steps, nullptr, 0, d_counters);
+  a.hist = d_hist;
+  a.hist_tgeo = d_tgeo;
+  a.hist_bins = n_bins;
+  a.hist_t_offset = t_offset;
+  a.hist_log_lo = log_lo;
+  a.hist_inv_log_width = (float)n_bins / (log_hi - log_lo);
+  cudaError_t e = pp::launch_propagate(a, ctx->tuning.block_threads, ctx->tuning.ctas_per_sm,
+                                       ctx->tuning.precise_math != 0, use_smem_grid(ctx),
+                                       ctx->num_sms, s, nullptr);
+  if (e != cudaSuccess) return cuda_error(e, "launch propagate kernel (histogram)");
+  return PP_OK;
+}
+
 PP_API int pp_launch_graph(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,
                            int64_t capacity, pp_counters* d_counters, void* stream) {
   int rc = validate_launch(ctx, n_steps, d_hits, capacity, d_counters);

@@ -117,6 +117,16 @@ struct LaunchArgs {
   pp_counters* counters;
   unsigned long long wait_limit_ns;        // bound on the TMA staging wait
 
+  // Histogram mode (hist != nullptr): instead of hit records, every hit adds
+  // its absorption weight to hist[s * (bins + 1)] (count) and to bin
+  // 1 + b of log10(t - tgeo[s] + hist_t_offset) on [hist_log_lo, hist_log_hi).
+  float* hist;
+  const float* hist_tgeo;
+  int hist_bins;
+  float hist_t_offset;
+  float hist_log_lo;
+  float hist_inv_log_width;
+
   uint32_t safety_offset;                  // shared-memory offset of the staged field
   uint32_t state_offset;                   // shared-memory offset of the warp state
   int warps_per_block;

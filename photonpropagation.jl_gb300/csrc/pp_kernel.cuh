@@ -407,8 +407,20 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         const float hdist = best.dist[lane];
         const double time = (double)t0 + (double)hdist / (double)med.y;
         const float abs_w = f_exp<kPrecise>(-f_div<kPrecise>(hdist, med.z));
-        record_hit(a, hpos, wl, hdir, hdist, idir, abs_w, time, p, (int)(key & 0xffffu) + 1,
-                   steps_taken, s, &overflowed);
+        if (a.hist) {
+          // arrival-time histogram of this source, weighted by absorption
+          const float tres = (float)(time - (double)__ldg(a.hist_tgeo + s));
+          const float u = log10f(fmaxf(tres + a.hist_t_offset, 1e-30f));
+          const int bin =
+              min(max((int)floorf((u - a.hist_log_lo) * a.hist_inv_log_width), 0), a.hist_bins - 1);
+          float* row = a.hist + (size_t)s * (size_t)(a.hist_bins + 1);
+          atomicAdd(row, abs_w);
+          atomicAdd(row + 1 + bin, abs_w);
+          atomicAdd(u64(&a.counters->n_hits), 1ull);
+        } else {
+          record_hit(a, hpos, wl, hdir, hdist, idir, abs_w, time, p, (int)(key & 0xffffu) + 1,
+                     steps_taken, s, &overflowed);
+        }
       }
       if (active) {
         steps_acc += (unsigned long long)steps_taken;

@@ -1,0 +1,700 @@
+// pp_mlp.cu -- the learned surrogate: a small MLP trained and evaluated with
+// hand-written BF16 tcgen05 kernels (FP32 accumulation in tensor memory).
+//
+// No counterpart in the reference: PhotonPropagation.jl evaluates an external
+// surrogate (PhotonSurrogateModel, examples/validation.jl:455,673-676) whose
+// weights are not part of the repository.  Here the network maps
+// source-module geometry to the expected hit count and a 64-bin arrival-time
+// distribution, trained on tables the MC kernel generates
+// (pp_launch_histogram).
+//
+// Network: x (n_in, zero-padded to a multiple of 16) -> 4 x [256, SiLU] ->
+// head (1 log-expected-count + 64 time logits, padded to 80).  Loss per sample
+// (Poisson + multinomial negative log-likelihood):
+//   L = exp(o0) - k*o0 - sum_b h_b * log softmax(o_1..64)_b.
+// Parameters are FP32 masters with BF16 copies for the tensor cores; Adam.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pp_internal.h"
+#include "pp_tc.cuh"
+
+using bf16 = __nv_bfloat16;
+
+namespace {
+
+constexpr int kTileM = 128;   // rows per CTA tile (tcgen05 M)
+constexpr int kKC = 64;       // K columns staged per iteration
+constexpr int kGemmThreads = 128;
+constexpr unsigned long long kWaitNs = 1000000000ull;
+
+enum GemmMode : int {
+  kStoreF32 = 0,     // C32 = acc + bias
+  kHiddenFwd = 1,    // Z16 = acc + bias, C16 = silu(acc + bias)
+  kBackwardDx = 2,   // C16 = acc * silu'(Zprev)
+  kAccumulateF32 = 3 // C32 += acc (atomic, split-K)
+};
+
+struct GemmParams {
+  const bf16* A;
+  long long lda;
+  int a_trans;  // element (m, k) = a_trans ? A[k*lda + m] : A[m*lda + k]
+  const bf16* B;
+  long long ldb;
+  int b_trans;  // element (n, k) = b_trans ? B[k*ldb + n] : B[n*ldb + k]
+  int M, N, K;  // N <= 256 and N % 16 == 0; K % 16 == 0
+  int k_per_split;
+  int mode;
+  const float* bias;
+  float* C32;
+  long long ldc;
+  bf16* C16;
+  long long ldc16;
+  bf16* Z16;
+  long long ldz;
+  const bf16* Zprev;
+  long long ldzp;
+  unsigned* err;
+};
+
+__host__ __device__ inline uint32_t tmem_cols_for(int n) {
+  uint32_t c = 32;
+  while (c < (uint32_t)n) c <<= 1;
+  return c;
+}
+
+// Stage rows [row0, row0 + rows_tile) x columns [k0, k0 + kKC) of an operand into
+// the core-matrix layout; rows >= rows_valid and columns >= k_end are zero.
+__device__ void stage_operand(unsigned char* dst, const bf16* __restrict__ src, long long ld,
+                              int trans, int row0, int rows_valid, int rows_tile, int k0,
+                              int k_end) {
+  constexpr int kb_n = kKC / 8;
+  if (!trans) {
+    const int nchunks = rows_tile * kb_n;
+    for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
+      const int r = c / kb_n, kb = c % kb_n;
+      const int gk = k0 + kb * 8;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (r < rows_valid && gk < k_end)
+        v = __ldg(reinterpret_cast<const uint4*>(src + (long long)(row0 + r) * ld + gk));
+      *reinterpret_cast<uint4*>(dst + pptc::core_offset(r, kb, kKC)) = v;
+    }
+  } else {
+    const int nchunks = (rows_tile / 8) * kKC;
+    for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
+      const int k = c % kKC, rg = c / kKC;
+      const int gk = k0 + k, r0 = rg * 8;
+      union {
+        uint4 u;
+        bf16 h[8];
+      } v;
+      v.u = make_uint4(0u, 0u, 0u, 0u);
+      if (gk < k_end) {
+        const bf16* p = src + (long long)gk * ld + row0 + r0;
+        if (r0 + 8 <= rows_valid) {
+          v.u = __ldg(reinterpret_cast<const uint4*>(p));
+        } else {
+          for (int j = 0; j < 8; ++j)
+            if (r0 + j < rows_valid) v.h[j] = p[j];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        *reinterpret_cast<bf16*>(dst + pptc::core_offset(r0 + j, k >> 3, kKC) + (k & 7) * 2) =
+            v.h[j];
+    }
+  }
+}
+
+// One CTA: a 128-row tile of D = A * B^T over the K range of blockIdx.z,
+// accumulated by tcgen05.mma in TMEM, then the fused epilogue.
+__global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constant__ GemmParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + kTileM * kKC * 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTileM;
+  const int kbeg = blockIdx.z * p.k_per_split;
+  const int kend = min(p.K, kbeg + p.k_per_split);
+  const uint32_t ncols = tmem_cols_for(p.N);
+
+  if (warp == 0) pptc::tmem_alloc(&tmem_slot, ncols);
+  if (threadIdx.x == 0) pptc::mbar_init(&bar, 1);
+  pptc::fence_before_sync();
+  __syncthreads();
+  pptc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = pptc::idesc_bf16(kTileM, p.N);
+  const uint32_t sbo = (kKC / 8) * 128;
+
+  bool ok = true;
+  uint32_t phase = 0;
+  for (int k0 = kbeg; k0 < kend; k0 += kKC) {
+    stage_operand(sA, p.A, p.lda, p.a_trans, m0, min(kTileM, p.M - m0), kTileM, k0, kend);
+    stage_operand(sB, p.B, p.ldb, p.b_trans, 0, p.N, p.N, k0, kend);
+    pptc::fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      pptc::fence_after_sync();
+      for (int s = 0; s < kKC / 16 && k0 + s * 16 < kend; ++s) {
+        const uint64_t ad = pptc::smem_desc(pptc::smem_u32(sA) + s * 256, 128, sbo);
+        const uint64_t bd = pptc::smem_desc(pptc::smem_u32(sB) + s * 256, 128, sbo);
+        pptc::mma_bf16(tmem, ad, bd, idesc, k0 > kbeg || s > 0);
+      }
+      pptc::mma_commit(&bar);
+    }
+    ok = pptc::mbar_wait(&bar, phase, kWaitNs);
+    phase ^= 1u;
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+  }
+  pptc::fence_after_sync();
+
+  if (ok && kend > kbeg) {
+    const int row = m0 + warp * 32 + lane;
+    const bool row_ok = row < p.M;
+    for (int c0 = 0; c0 < p.N; c0 += 32) {
+      float v[32];
+      pptc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (!row_ok) continue;
+#pragma unroll 4
+      for (int i = 0; i < 32; ++i) {
+        const int col = c0 + i;
+        if (col >= p.N) break;
+        const float acc = v[i];
+        switch (p.mode) {
+          case kStoreF32:
+            p.C32[(long long)row * p.ldc + col] = acc + (p.bias ? p.bias[col] : 0.0f);
+            break;
+          case kHiddenFwd: {
+            const float z = acc + p.bias[col];
+            p.Z16[(long long)row * p.ldz + col] = __float2bfloat16(z);
+            p.C16[(long long)row * p.ldc16 + col] = __float2bfloat16(pptc::silu(z));
+            break;
+          }
+          case kBackwardDx: {
+            const float z = __bfloat162float(p.Zprev[(long long)row * p.ldzp + col]);
+            p.C16[(long long)row * p.ldc16 + col] = __float2bfloat16(acc * pptc::silu_grad(z));
+            break;
+          }
+          default:
+            atomicAdd(p.C32 + (long long)row * p.ldc + col, acc);
+            break;
+        }
+      }
+    }
+  }
+  pptc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) pptc::tmem_dealloc(tmem, ncols);
+  if (!ok && threadIdx.x == 0) atomicOr(p.err, 1u);
+}
+
+// Features (n x n_in, FP32) -> zero-padded BF16 rows of in_pad.
+__global__ void pack_input_kernel(const float* __restrict__ x, int n, int n_in, int in_pad,
+                                  bf16* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)n * in_pad) return;
+  const long long r = i / in_pad;
+  const int c = (int)(i % in_pad);
+  out[i] = __float2bfloat16(c < n_in ? x[r * n_in + c] : 0.0f);
+}
+
+// Poisson + multinomial NLL per sample (one warp per sample) and its gradient
+// with respect to the head outputs.
+__global__ void loss_kernel(const float* __restrict__ O, long long ldo, int B,
+                            const float* __restrict__ count, const float* __restrict__ hist,
+                            int nb, float inv_b, float time_weight, bf16* __restrict__ dO16,
+                            float* __restrict__ dO32, long long ldd, int out_pad,
+                            float* __restrict__ loss) {
+  const int warps = blockDim.x >> 5;
+  const int row = blockIdx.x * warps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= B) return;
+  const float* o = O + (long long)row * ldo;
+  const float o0 = fminf(o[0], 30.0f);
+  const float lam = __expf(o0);
+  const float k = count[row];
+  float mx = -INFINITY;
+  for (int j = lane; j < nb; j += 32) mx = fmaxf(mx, o[1 + j]);
+  for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, s));
+  float se = 0.0f, sh = 0.0f, shx = 0.0f;
+  for (int j = lane; j < nb; j += 32) {
+    const float x = o[1 + j] - mx;
+    const float h = hist[(long long)row * nb + j];
+    se += __expf(x);
+    sh += h;
+    shx += h * x;
+  }
+  for (int s = 16; s > 0; s >>= 1) {
+    se += __shfl_xor_sync(0xffffffffu, se, s);
+    sh += __shfl_xor_sync(0xffffffffu, sh, s);
+    shx += __shfl_xor_sync(0xffffffffu, shx, s);
+  }
+  const float lse = __logf(se);
+  bf16* d16 = dO16 + (long long)row * ldd;
+  float* d32 = dO32 + (long long)row * ldd;
+  for (int j = lane; j < out_pad; j += 32) {
+    float g = 0.0f;
+    if (j == 0) {
+      g = (lam - k) * inv_b;
+    } else if (j <= nb) {
+      const float pj = __expf(o[j] - mx - lse);
+      g = (sh * pj - hist[(long long)row * nb + j - 1]) * inv_b * time_weight;
+    }
+    d16[j] = __float2bfloat16(g);
+    d32[j] = g;
+  }
+  if (lane == 0) {
+    const float lc = lam - k * o0;
+    const float lt = -(shx - sh * lse);
+    atomicAdd(loss, (lc + time_weight * lt) * inv_b);
+  }
+}
+
+// out[c] += sum over rows of X[r][c] (bias gradients).
+template <typename T>
+__global__ void colsum_kernel(const T* __restrict__ X, int rows, int cols, long long ld,
+                              float* __restrict__ out) {
+  const int c = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int ry = threadIdx.x >> 5;
+  float s = 0.0f;
+  if (c < cols)
+    for (int r = blockIdx.y * 8 + ry; r < rows; r += gridDim.y * 8) s += (float)X[(long long)r * ld + c];
+  __shared__ float red[8][33];
+  red[ry][threadIdx.x & 31] = s;
+  __syncthreads();
+  if (ry == 0 && c < cols) {
+    float t = 0.0f;
+    for (int i = 0; i < 8; ++i) t += red[i][threadIdx.x & 31];
+    atomicAdd(out + c, t);
+  }
+}
+
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v, long long n, float lr,
+                            float b1, float b2, float eps, float bc1, float bc2,
+                            bf16* __restrict__ w16) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.0f - b1) * gi;
+  const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  w[i] = wi;
+  w16[i] = __float2bfloat16(wi);
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* __restrict__ y) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __float2bfloat16(x[i]);
+}
+
+int fail(int code, const std::string& m) { return pp::report_error(code, m); }
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(PP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Shared memory per CTA.  Requesting at least 80 KB when the accumulator takes
+// 256 TMEM columns keeps at most two CTAs (2 x 256 = all 512 columns) on an
+// SM, so tensor-memory allocations never wait on each other.
+constexpr size_t kGemmSmemMax = 80 * 1024;
+
+cudaError_t launch_gemm(const GemmParams& p, cudaStream_t s) {
+  size_t smem = (size_t)kTileM * kKC * 2 + (size_t)p.N * kKC * 2;
+  if (tmem_cols_for(p.N) > 128) smem = std::max(smem, kGemmSmemMax);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kGemmSmemMax);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int splits = (p.K + p.k_per_split - 1) / p.k_per_split;
+  dim3 grid((p.M + kTileM - 1) / kTileM, 1, splits);
+  gemm_kernel<<<grid, kGemmThreads, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+inline int pad16(int x) { return (x + 15) & ~15; }
+inline long long pad8ll(long long x) { return (x + 7) & ~7LL; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// The network object.
+struct pp_mlp {
+  int device = 0;
+  int n_in = 8, in_pad = 16, hidden = 256, n_layers = 4, n_out = 65, out_pad = 80, n_bins = 64;
+  int max_batch = 0;
+  long long n_params = 0;
+  std::vector<long long> off_w, off_b;  // per layer (n_layers hidden + head)
+  std::vector<int> rows, cols;          // W_l is rows x cols (out_pad x in_pad)
+  float *P = nullptr, *G = nullptr, *Mo = nullptr, *Vo = nullptr;
+  bf16* P16 = nullptr;
+  bf16* X0 = nullptr;
+  std::vector<bf16*> Z, Y;
+  float* O = nullptr;
+  bf16* dO16 = nullptr;
+  float* dO32 = nullptr;
+  bf16* dZ[2] = {nullptr, nullptr};
+  float* loss = nullptr;
+  unsigned* err = nullptr;
+  long long step = 0;
+  float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f, time_weight = 1.0f;
+};
+
+namespace {
+
+void mlp_free(pp_mlp* m) {
+  cudaFree(m->P); cudaFree(m->G); cudaFree(m->Mo); cudaFree(m->Vo); cudaFree(m->P16);
+  cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16); cudaFree(m->dO32);
+  cudaFree(m->dZ[0]); cudaFree(m->dZ[1]); cudaFree(m->loss); cudaFree(m->err);
+  for (auto* p : m->Z) cudaFree(p);
+  for (auto* p : m->Y) cudaFree(p);
+}
+
+GemmParams base_params(pp_mlp* m) {
+  GemmParams p{};
+  p.err = m->err;
+  return p;
+}
+
+int mlp_forward(pp_mlp* m, const float* d_x, int B, cudaStream_t s) {
+  const long long nin = (long long)B * m->in_pad;
+  pack_input_kernel<<<(unsigned)((nin + 255) / 256), 256, 0, s>>>(d_x, B, m->n_in, m->in_pad,
+                                                                  m->X0);
+  const bf16* x = m->X0;
+  long long ldx = m->in_pad;
+  int kin = m->in_pad;
+  for (int l = 0; l < m->n_layers; ++l) {
+    GemmParams p = base_params(m);
+    p.A = x; p.lda = ldx; p.a_trans = 0;
+    p.B = m->P16 + m->off_w[l]; p.ldb = m->cols[l]; p.b_trans = 0;
+    p.M = B; p.N = m->hidden; p.K = kin; p.k_per_split = kin;
+    p.mode = kHiddenFwd; p.bias = m->P + m->off_b[l];
+    p.Z16 = m->Z[l]; p.ldz = m->hidden; p.C16 = m->Y[l]; p.ldc16 = m->hidden;
+    cudaError_t e = launch_gemm(p, s);
+    if (e != cudaSuccess) return cuda_fail(e, "mlp forward gemm");
+    x = m->Y[l]; ldx = m->hidden; kin = m->hidden;
+  }
+  GemmParams p = base_params(m);
+  const int L = m->n_layers;
+  p.A = x; p.lda = ldx; p.a_trans = 0;
+  p.B = m->P16 + m->off_w[L]; p.ldb = m->cols[L]; p.b_trans = 0;
+  p.M = B; p.N = m->out_pad; p.K = kin; p.k_per_split = kin;
+  p.mode = kStoreF32; p.bias = m->P + m->off_b[L]; p.C32 = m->O; p.ldc = m->out_pad;
+  cudaError_t e = launch_gemm(p, s);
+  if (e != cudaSuccess) return cuda_fail(e, "mlp head gemm");
+  return PP_OK;
+}
+
+int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(m->G, 0, sizeof(float) * m->n_params, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->loss, 0, sizeof(float), s);
+  if (e != cudaSuccess) return cuda_fail(e, "zero gradients");
+  const int L = m->n_layers;
+  loss_kernel<<<(B + 7) / 8, 256, 0, s>>>(m->O, m->out_pad, B, d_count, d_hist, m->n_bins,
+                                          1.0f / (float)B, m->time_weight, m->dO16, m->dO32,
+                                          m->out_pad, m->out_pad, m->loss);
+  const int ksplit = 512;
+  auto colsum16 = [&](const bf16* X, int cols, long long ld, float* out) {
+    dim3 g((cols + 31) / 32, std::min(64, (B + 7) / 8));
+    colsum_kernel<bf16><<<g, 256, 0, s>>>(X, B, cols, ld, out);
+  };
+  // head
+  {
+    dim3 g((m->out_pad + 31) / 32, std::min(64, (B + 7) / 8));
+    colsum_kernel<float><<<g, 256, 0, s>>>(m->dO32, B, m->out_pad, m->out_pad, m->G + m->off_b[L]);
+    GemmParams p = base_params(m);  // dW_head[o][i] += sum_b dO[b][o] Y[b][i]
+    p.A = m->dO16; p.lda = m->out_pad; p.a_trans = 1;
+    p.B = m->Y[L - 1]; p.ldb = m->hidden; p.b_trans = 1;
+    p.M = m->out_pad; p.N = m->hidden; p.K = B; p.k_per_split = ksplit;
+    p.mode = kAccumulateF32; p.C32 = m->G + m->off_w[L]; p.ldc = m->cols[L];
+    if ((e = launch_gemm(p, s)) != cudaSuccess) return cuda_fail(e, "dW head");
+    GemmParams q = base_params(m);  // dZ[L-1] = (dO W_head) * silu'(Z[L-1])
+    q.A = m->dO16; q.lda = m->out_pad; q.a_trans = 0;
+    q.B = m->P16 + m->off_w[L]; q.ldb = m->cols[L]; q.b_trans = 1;
+    q.M = B; q.N = m->hidden; q.K = m->out_pad; q.k_per_split = m->out_pad;
+    q.mode = kBackwardDx; q.Zprev = m->Z[L - 1]; q.ldzp = m->hidden;
+    q.C16 = m->dZ[0]; q.ldc16 = m->hidden;
+    if ((e = launch_gemm(q, s)) != cudaSuccess) return cuda_fail(e, "dX head");
+  }
+  int cur = 0;
+  for (int l = L - 1; l >= 0; --l) {
+    const bf16* xin = l > 0 ? m->Y[l - 1] : m->X0;
+    const long long ldx = l > 0 ? m->hidden : m->in_pad;
+    const int nin = l > 0 ? m->hidden : m->in_pad;
+    colsum16(m->dZ[cur], m->hidden, m->hidden, m->G + m->off_b[l]);
+    GemmParams p = base_params(m);  // dW_l[o][i] += sum_b dZ[b][o] x[b][i]
+    p.A = m->dZ[cur]; p.lda = m->hidden; p.a_trans = 1;
+    p.B = xin; p.ldb = ldx; p.b_trans = 1;
+    p.M = m->hidden; p.N = nin; p.K = B; p.k_per_split = ksplit;
+    p.mode = kAccumulateF32; p.C32 = m->G + m->off_w[l]; p.ldc = m->cols[l];
+    if ((e = launch_gemm(p, s)) != cudaSuccess) return cuda_fail(e, "dW hidden");
+    if (l == 0) break;
+    GemmParams q = base_params(m);  // dZ[l-1] = (dZ_l W_l) * silu'(Z[l-1])
+    q.A = m->dZ[cur]; q.lda = m->hidden; q.a_trans = 0;
+    q.B = m->P16 + m->off_w[l]; q.ldb = m->cols[l]; q.b_trans = 1;
+    q.M = B; q.N = m->hidden; q.K = m->hidden; q.k_per_split = m->hidden;
+    q.mode = kBackwardDx; q.Zprev = m->Z[l - 1]; q.ldzp = m->hidden;
+    q.C16 = m->dZ[cur ^ 1]; q.ldc16 = m->hidden;
+    if ((e = launch_gemm(q, s)) != cudaSuccess) return cuda_fail(e, "dX hidden");
+    cur ^= 1;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "mlp backward");
+  return PP_OK;
+}
+
+int check_err(pp_mlp* m, cudaStream_t s) {
+  unsigned h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, m->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "mlp");
+  if (h) {
+    cudaMemsetAsync(m->err, 0, sizeof(unsigned), s);
+    return fail(PP_ERR_TIMEOUT, "a tensor-core wait timed out");
+  }
+  return PP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+PP_API int pp_mlp_create(pp_mlp** out, int32_t device, int32_t n_in, int32_t hidden,
+                         int32_t n_layers, int32_t n_bins, int32_t max_batch, uint64_t seed) {
+  if (!out) return fail(PP_ERR_INVALID, "null output");
+  *out = nullptr;
+  if (n_in < 1 || n_in > 240 || hidden < 16 || hidden > 256 || hidden % 16 || n_layers < 1 ||
+      n_layers > 16 || n_bins < 1 || n_bins + 1 > 256 || max_batch < 1)
+    return fail(PP_ERR_INVALID, "mlp dims: 1<=n_in<=240, hidden multiple of 16 <= 256, "
+                                "n_bins <= 255, max_batch >= 1");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return fail(PP_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  cudaSetDevice(device);
+  pp_mlp* m = new pp_mlp();
+  m->device = device;
+  m->n_in = n_in;
+  m->in_pad = pad16(n_in);
+  m->hidden = hidden;
+  m->n_layers = n_layers;
+  m->n_bins = n_bins;
+  m->n_out = n_bins + 1;
+  m->out_pad = pad16(m->n_out);
+  m->max_batch = max_batch;
+  long long off = 0;
+  for (int l = 0; l <= n_layers; ++l) {
+    const int r = l < n_layers ? hidden : m->out_pad;
+    const int c = l == 0 ? m->in_pad : hidden;
+    m->rows.push_back(r);
+    m->cols.push_back(c);
+    m->off_w.push_back(off);
+    off = pad8ll(off + (long long)r * c);
+    m->off_b.push_back(off);
+    off = pad8ll(off + r);
+  }
+  m->n_params = off;
+  // He-style initialisation of the real (unpadded) weights; zeros elsewhere.
+  std::vector<float> h(off, 0.0f);
+  uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
+  auto rnd = [&]() {  // xorshift64*, uniform (-1, 1)
+    st ^= st >> 12; st ^= st << 25; st ^= st >> 27;
+    return (double)((st * 2685821657736338717ull) >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  };
+  for (int l = 0; l <= n_layers; ++l) {
+    const int fan_in = l == 0 ? n_in : hidden;
+    const int rows_real = l < n_layers ? hidden : m->n_out;
+    const double a = std::sqrt(6.0 / fan_in) * (l < n_layers ? 1.0 : 0.1);
+    for (int r = 0; r < rows_real; ++r)
+      for (int c = 0; c < fan_in; ++c) h[m->off_w[l] + (long long)r * m->cols[l] + c] = (float)(a * rnd());
+  }
+  const size_t pb = sizeof(float) * off;
+  const long long Bn = max_batch;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  A((void**)&m->P, pb); A((void**)&m->G, pb); A((void**)&m->Mo, pb); A((void**)&m->Vo, pb);
+  A((void**)&m->P16, sizeof(bf16) * off);
+  A((void**)&m->X0, sizeof(bf16) * Bn * m->in_pad);
+  m->Z.assign(n_layers, nullptr);
+  m->Y.assign(n_layers, nullptr);
+  for (int l = 0; l < n_layers; ++l) {
+    A((void**)&m->Z[l], sizeof(bf16) * Bn * hidden);
+    A((void**)&m->Y[l], sizeof(bf16) * Bn * hidden);
+  }
+  A((void**)&m->O, sizeof(float) * Bn * m->out_pad);
+  A((void**)&m->dO16, sizeof(bf16) * Bn * m->out_pad);
+  A((void**)&m->dO32, sizeof(float) * Bn * m->out_pad);
+  A((void**)&m->dZ[0], sizeof(bf16) * Bn * hidden);
+  A((void**)&m->dZ[1], sizeof(bf16) * Bn * hidden);
+  A((void**)&m->loss, sizeof(float));
+  A((void**)&m->err, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemcpy(m->P, h.data(), pb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(m->Mo, 0, pb);
+  if (e == cudaSuccess) e = cudaMemset(m->Vo, 0, pb);
+  if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(unsigned));
+  if (e == cudaSuccess) {
+    to_bf16_kernel<<<(unsigned)((off + 255) / 256), 256>>>(m->P, off, m->P16);
+    e = cudaDeviceSynchronize();
+  }
+  if (e != cudaSuccess) {
+    mlp_free(m);
+    delete m;
+    return cuda_fail(e, "pp_mlp_create");
+  }
+  *out = m;
+  return PP_OK;
+}
+
+PP_API int pp_mlp_destroy(pp_mlp* m) {
+  if (!m) return PP_OK;
+  cudaSetDevice(m->device);
+  cudaDeviceSynchronize();
+  mlp_free(m);
+  delete m;
+  return PP_OK;
+}
+
+PP_API int pp_mlp_num_params(const pp_mlp* m, int64_t* n) {
+  if (!m || !n) return fail(PP_ERR_INVALID, "null argument");
+  *n = m->n_params;
+  return PP_OK;
+}
+
+// Offsets (in floats) of W_l and b_l in the packed parameter vector and the
+// padded shape of W_l (rows x cols, row-major).
+PP_API int pp_mlp_layout(const pp_mlp* m, int32_t layer, int64_t* off_w, int64_t* off_b,
+                         int32_t* rows, int32_t* cols) {
+  if (!m || layer < 0 || layer > m->n_layers) return fail(PP_ERR_INVALID, "bad layer");
+  if (off_w) *off_w = m->off_w[layer];
+  if (off_b) *off_b = m->off_b[layer];
+  if (rows) *rows = m->rows[layer];
+  if (cols) *cols = m->cols[layer];
+  return PP_OK;
+}
+
+PP_API int pp_mlp_get_params(const pp_mlp* m, float* host, int64_t n) {
+  if (!m || !host || n != m->n_params) return fail(PP_ERR_INVALID, "bad parameter buffer");
+  cudaSetDevice(m->device);
+  cudaError_t e = cudaMemcpy(host, m->P, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? PP_OK : cuda_fail(e, "pp_mlp_get_params");
+}
+
+PP_API int pp_mlp_set_params(pp_mlp* m, const float* host, int64_t n) {
+  if (!m || !host || n != m->n_params) return fail(PP_ERR_INVALID, "bad parameter buffer");
+  cudaSetDevice(m->device);
+  cudaError_t e = cudaMemcpy(m->P, host, sizeof(float) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    to_bf16_kernel<<<(unsigned)((n + 255) / 256), 256>>>(m->P, n, m->P16);
+    e = cudaDeviceSynchronize();
+  }
+  return e == cudaSuccess ? PP_OK : cuda_fail(e, "pp_mlp_set_params");
+}
+
+// Forward pass of the training graph: raw head outputs (B x out_pad, FP32,
+// column 0 = log expected count, 1..n_bins = time logits) into d_out.
+PP_API int pp_mlp_forward(pp_mlp* m, const float* d_x, int32_t B, float* d_out, void* stream) {
+  if (!m || !d_x || !d_out || B < 1 || B > m->max_batch) return fail(PP_ERR_INVALID, "bad arguments");
+  cudaSetDevice(m->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = mlp_forward(m, d_x, B, s);
+  if (rc != PP_OK) return rc;
+  cudaError_t e = cudaMemcpyAsync(d_out, m->O, sizeof(float) * (size_t)B * m->out_pad,
+                                  cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy head outputs");
+  return check_err(m, s);
+}
+
+// Loss and gradient (no update): gradients of the packed parameters to host.
+PP_API int pp_mlp_loss_grad(pp_mlp* m, const float* d_x, const float* d_count,
+                            const float* d_hist, int32_t B, float* host_grad, float* host_loss,
+                            void* stream) {
+  if (!m || !d_x || !d_count || !d_hist || B < 1 || B > m->max_batch)
+    return fail(PP_ERR_INVALID, "bad arguments");
+  cudaSetDevice(m->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = mlp_forward(m, d_x, B, s);
+  if (rc == PP_OK) rc = mlp_backward(m, d_count, d_hist, B, s);
+  if (rc != PP_OK) return rc;
+  cudaError_t e = cudaSuccess;
+  if (host_grad) e = cudaMemcpyAsync(host_grad, m->G, sizeof(float) * m->n_params,
+                                     cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && host_loss)
+    e = cudaMemcpyAsync(host_loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "copy gradients");
+  return check_err(m, s);
+}
+
+// One Adam step on a batch (forward, backward, update), asynchronous on
+// `stream`; the batch loss is left in device memory (pp_mlp_last_loss).
+PP_API int pp_mlp_train_step(pp_mlp* m, const float* d_x, const float* d_count,
+                             const float* d_hist, int32_t B, float lr, void* stream) {
+  if (!m || !d_x || !d_count || !d_hist || B < 1 || B > m->max_batch)
+    return fail(PP_ERR_INVALID, "bad arguments");
+  cudaSetDevice(m->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = mlp_forward(m, d_x, B, s);
+  if (rc == PP_OK) rc = mlp_backward(m, d_count, d_hist, B, s);
+  if (rc != PP_OK) return rc;
+  m->step += 1;
+  const float bc1 = 1.0f - std::pow(m->b1, (float)m->step);
+  const float bc2 = 1.0f - std::pow(m->b2, (float)m->step);
+  adam_kernel<<<(unsigned)((m->n_params + 255) / 256), 256, 0, s>>>(
+      m->P, m->G, m->Mo, m->Vo, m->n_params, lr, m->b1, m->b2, m->eps, bc1, bc2, m->P16);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? PP_OK : cuda_fail(e, "adam");
+}
+
+PP_API int pp_mlp_last_loss(pp_mlp* m, float* host_loss) {
+  if (!m || !host_loss) return fail(PP_ERR_INVALID, "null argument");
+  cudaSetDevice(m->device);
+  cudaError_t e = cudaMemcpy(host_loss, m->loss, sizeof(float), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "read loss");
+  return check_err(m, nullptr);
+}
+
+// One tcgen05 GEMM for tests: C (M x N, FP32) = A (M x K) * B^T with B given
+// as N x K (both BF16, row-major, device memory); N <= 256, N and K multiples
+// of 16, lda/ldb multiples of 8.
+PP_API int pp_mlp_gemm_test(const void* d_a, int64_t lda, int32_t a_trans, const void* d_b,
+                            int64_t ldb, int32_t b_trans, int32_t M, int32_t N, int32_t K,
+                            int32_t k_split, float* d_c, int64_t ldc, void* stream) {
+  if (!d_a || !d_b || !d_c || M < 1 || N < 16 || N > 256 || N % 16 || K < 16 || K % 16 ||
+      lda % 8 || ldb % 8)
+    return fail(PP_ERR_INVALID, "bad gemm arguments");
+  unsigned* err = nullptr;
+  cudaError_t e = cudaMalloc(&err, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(unsigned));
+  if (e != cudaSuccess) return cuda_fail(e, "gemm test");
+  GemmParams p{};
+  p.A = (const bf16*)d_a; p.lda = lda; p.a_trans = a_trans;
+  p.B = (const bf16*)d_b; p.ldb = ldb; p.b_trans = b_trans;
+  p.M = M; p.N = N; p.K = K;
+  p.k_per_split = k_split > 0 ? ((K + k_split - 1) / k_split + kKC - 1) / kKC * kKC : K;
+  p.mode = k_split > 0 ? kAccumulateF32 : kStoreF32;
+  p.C32 = d_c; p.ldc = ldc; p.err = err;
+  e = launch_gemm(p, (cudaStream_t)stream);
+  unsigned h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (e != cudaSuccess) return cuda_fail(e, "gemm test");
+  return h ? fail(PP_ERR_TIMEOUT, "tensor-core wait timed out") : PP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,229 @@
+"""Learned surrogate for module expectations (C3/C4 of the benchmark plan).
+
+* ``pair_features`` / ``sample_pairs``: source-module geometry (distance
+  log-uniform on [5, 300] m, module direction and emitter direction uniform on
+  the sphere) and its 8 input features.
+* ``generate_tables``: one Monte-Carlo run per pair with the propagation
+  kernel in histogram mode: expected hits (absorption-weighted) and a 64-bin
+  histogram of log10(t_res + 21 ns) over residual times [-20, 2000] ns, with
+  t_res = t - (d - r) / v_group(800 nm) as the reference's calc_time_residual!
+  (src/calc.jl) defines it.
+* ``MLP``: the network of csrc/pp_mlp.cu (BF16 tcgen05 forward/backward,
+  Adam), trained by ``train``.
+
+There is no surrogate in the reference repository (it loads an external
+PhotonSurrogateModel, examples/validation.jl:455,673-676).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_float, c_int32, c_int64, c_void_p
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import check
+from .medium import CascadiaMediumProperties
+from .sources import ExtendedCherenkovEmitter, LongitudinalParameterisation, to_records
+from .spectrum import make_cherenkov_spectrum
+from .targets import HomogeneousDetector, Spherical
+
+N_FEATURES = 8
+N_BINS = 64
+T_OFFSET = 21.0                 # ns: log10(t_res + 21) maps [-20, 2000] to [0, log10 2021]
+LOG_T_LO = 0.0
+LOG_T_HI = float(np.log10(2021.0))
+D_MIN, D_MAX = 5.0, 300.0
+MODULE_RADIUS = 0.2159
+CASCADE = LongitudinalParameterisation(2.0, 0.63, 0.36)
+
+
+def _unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+@dataclass
+class Pairs:
+    distance: np.ndarray     # m
+    module_dir: np.ndarray   # unit vector source -> module
+    emitter_dir: np.ndarray  # unit emitter axis
+    spectrum_id: np.ndarray  # 0 = Frank-Tamm on 300-800 nm
+
+    def __len__(self):
+        return int(self.distance.shape[0])
+
+    def subset(self, idx):
+        return Pairs(self.distance[idx], self.module_dir[idx], self.emitter_dir[idx],
+                     self.spectrum_id[idx])
+
+
+def sample_pairs(n: int, seed: int = 0) -> Pairs:
+    rng = np.random.default_rng(seed)
+    d = np.exp(rng.uniform(np.log(D_MIN), np.log(D_MAX), n))
+    return Pairs(d, _unit(rng, n), _unit(rng, n), np.zeros(n, np.int32))
+
+
+def pair_features(p: Pairs) -> np.ndarray:
+    """[log-distance (scaled), cos/sin of the emitter-to-module angle, cos/sin of
+    the module azimuth about the emitter axis, cos/sin of the emitter azimuth,
+    spectrum id]."""
+    e, m = p.emitter_dir, p.module_dir
+    ct = np.clip(np.sum(e * m, axis=1), -1.0, 1.0)
+    st = np.sqrt(np.maximum(0.0, 1.0 - ct * ct))
+    phi_m = np.arctan2(m[:, 1], m[:, 0])
+    phi_e = np.arctan2(e[:, 1], e[:, 0])
+    ld = (np.log10(p.distance) - 1.34) / 0.45
+    x = np.stack([ld, ct, st, np.cos(phi_m), np.sin(phi_m), np.cos(phi_e), np.sin(phi_e),
+                  p.spectrum_id.astype(np.float64)], axis=1)
+    return x.astype(np.float32)
+
+
+def in_training_range(p: Pairs) -> np.ndarray:
+    return (p.distance >= D_MIN) & (p.distance <= D_MAX) & (p.spectrum_id == 0)
+
+
+def generate_tables(pairs: Pairs, photons: int, seed: int = 1, ctx=None, medium=None,
+                    spectrum=None, device: int = 0, chunk: int = 262144, n_steps: int = 15):
+    """Expected hits and time histograms of every pair (one MC run each).
+
+    The module sits at the origin; pair i is a cascade at -d_i * module_dir_i
+    pointing along emitter_dir_i, so all pairs share one target and run in one
+    persistent launch per chunk.  Returns (counts [n], hists [n x 64]) as numpy
+    arrays for `photons` photons per pair."""
+    import torch
+    from .context import Context
+    medium = medium or CascadiaMediumProperties()
+    spectrum = spectrum or make_cherenkov_spectrum((300.0, 800.0), medium)
+    own = ctx is None
+    ctx = ctx or Context(device)
+    from .propsetup import PhotonPropSetup
+    tgt = HomogeneousDetector(Spherical([0.0, 0.0, 0.0], MODULE_RADIUS), 1.0, 1)
+    base = PhotonPropSetup([ExtendedCherenkovEmitter([0, 0, -10], [0, 0, 1], 0.0, 1, CASCADE)],
+                           [tgt], medium, spectrum, seed)
+    base.upload(ctx)
+    v800 = float(medium.group_velocity(800.0))
+    n = len(pairs)
+    counts = np.zeros(n, np.float32)
+    hists = np.zeros((n, N_BINS), np.float32)
+    ctr = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    for lo in range(0, n, chunk):
+        hi = min(n, lo + chunk)
+        sub = pairs.subset(slice(lo, hi))
+        pos = -sub.distance[:, None] * sub.module_dir
+        srcs = [ExtendedCherenkovEmitter(pos[i], sub.emitter_dir[i], 0.0, photons, CASCADE)
+                for i in range(hi - lo)]
+        recs = to_records(srcs)
+        ctx.set_sources(recs, hi - lo, 1.0)
+        tgeo = torch.tensor((sub.distance - MODULE_RADIUS) / v800, dtype=torch.float32,
+                            device="cuda")
+        hist = torch.empty((hi - lo, N_BINS + 1), dtype=torch.float32, device="cuda")
+        check(ctx._lib.pp_launch_histogram(ctx.ptr, seed + lo, n_steps, c_void_p(tgeo.data_ptr()),
+                                           c_void_p(hist.data_ptr()), N_BINS, T_OFFSET, LOG_T_LO,
+                                           LOG_T_HI, c_void_p(ctr.data_ptr()), None),
+              "pp_launch_histogram")
+        h = hist.cpu().numpy()
+        counts[lo:hi] = h[:, 0]
+        hists[lo:hi] = h[:, 1:]
+    if own:
+        ctx.close()
+    return counts, hists
+
+
+class MLP:
+    """Handle on a pp_mlp (parameters and optimiser state live on the device)."""
+
+    def __init__(self, device=0, n_in=N_FEATURES, hidden=256, n_layers=4, n_bins=N_BINS,
+                 max_batch=8192, seed=0):
+        self._lib = _lib.load()
+        p = c_void_p()
+        check(self._lib.pp_mlp_create(byref(p), device, n_in, hidden, n_layers, n_bins,
+                                      max_batch, seed), "pp_mlp_create")
+        self.ptr = p
+        self.n_in, self.hidden, self.n_layers, self.n_bins = n_in, hidden, n_layers, n_bins
+        self.max_batch = max_batch
+        n = c_int64()
+        check(self._lib.pp_mlp_num_params(self.ptr, byref(n)))
+        self.n_params = n.value
+
+    def close(self):
+        if getattr(self, "ptr", None) and self.ptr.value:
+            self._lib.pp_mlp_destroy(self.ptr)
+            self.ptr = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def layout(self, layer):
+        ow, ob, r, c = c_int64(), c_int64(), c_int32(), c_int32()
+        check(self._lib.pp_mlp_layout(self.ptr, layer, byref(ow), byref(ob), byref(r), byref(c)))
+        return ow.value, ob.value, r.value, c.value
+
+    def params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        check(self._lib.pp_mlp_get_params(self.ptr, out.ctypes.data_as(ctypes.POINTER(c_float)),
+                                          self.n_params))
+        return out
+
+    def set_params(self, v: np.ndarray) -> None:
+        v = np.ascontiguousarray(v, np.float32)
+        check(self._lib.pp_mlp_set_params(self.ptr, v.ctypes.data_as(ctypes.POINTER(c_float)),
+                                          self.n_params))
+
+    def unpack(self, flat):
+        W, b = [], []
+        for l in range(self.n_layers + 1):
+            ow, ob, r, c = self.layout(l)
+            W.append(flat[ow:ow + r * c].reshape(r, c))
+            b.append(flat[ob:ob + r])
+        return W, b
+
+    def forward(self, x_dev, B, out_dev, stream=0):
+        check(self._lib.pp_mlp_forward(self.ptr, c_void_p(x_dev), B, c_void_p(out_dev),
+                                       c_void_p(stream)), "pp_mlp_forward")
+
+    def loss_grad(self, x_dev, count_dev, hist_dev, B):
+        g = np.empty(self.n_params, np.float32)
+        loss = c_float()
+        check(self._lib.pp_mlp_loss_grad(self.ptr, c_void_p(x_dev), c_void_p(count_dev),
+                                         c_void_p(hist_dev), B,
+                                         g.ctypes.data_as(ctypes.POINTER(c_float)), byref(loss),
+                                         None), "pp_mlp_loss_grad")
+        return loss.value, g
+
+    def train_step(self, x_dev, count_dev, hist_dev, B, lr, stream=0):
+        check(self._lib.pp_mlp_train_step(self.ptr, c_void_p(x_dev), c_void_p(count_dev),
+                                          c_void_p(hist_dev), B, float(lr), c_void_p(stream)),
+              "pp_mlp_train_step")
+
+    def last_loss(self) -> float:
+        v = c_float()
+        check(self._lib.pp_mlp_last_loss(self.ptr, byref(v)), "pp_mlp_last_loss")
+        return v.value
+
+
+def train(mlp: MLP, x, counts, hists, steps: int, batch: int = 8192, lr: float = 1e-3,
+          seed: int = 0, log_every: int = 0):
+    """Adam on (features, expected hits, time histograms) held in device memory
+    (torch tensors); returns the list of (step, loss) logged."""
+    import torch
+    n = x.shape[0]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    log = []
+    bx = torch.empty((batch, x.shape[1]), dtype=torch.float32, device="cuda")
+    bc = torch.empty((batch,), dtype=torch.float32, device="cuda")
+    bh = torch.empty((batch, hists.shape[1]), dtype=torch.float32, device="cuda")
+    for s in range(steps):
+        idx = torch.randint(0, n, (batch,), device="cuda", generator=g)
+        torch.index_select(x, 0, idx, out=bx)
+        torch.index_select(counts, 0, idx, out=bc)
+        torch.index_select(hists, 0, idx, out=bh)
+        mlp.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), batch, lr)
+        if log_every and (s % log_every == 0 or s == steps - 1):
+            log.append((s, mlp.last_loss()))
+    return log

@@ -1,0 +1,133 @@
+"""Surrogate MLP: the CPU oracle pinned by finite differences, the tcgen05 GEMM
+against numpy, and device gradients against the oracle tensor by tensor."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import mlp_oracle  # noqa: E402
+
+
+def _tiny_net(rng, n_in=3, hidden=5, layers=2, n_bins=4):
+    W, b = [], []
+    sizes = [n_in] + [hidden] * layers
+    for l in range(layers):
+        W.append(rng.normal(0, 0.6, (hidden, sizes[l])))
+        b.append(rng.normal(0, 0.1, hidden))
+    W.append(rng.normal(0, 0.3, (n_bins + 1, hidden)))
+    b.append(rng.normal(0, 0.1, n_bins + 1))
+    return W, b
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    W, b = _tiny_net(rng)
+    x = rng.normal(size=(7, 3))
+    count = rng.poisson(3.0, 7).astype(np.float64)
+    hist = rng.poisson(2.0, (7, 4)).astype(np.float64)
+
+    def loss_of(Wl, bl):
+        o = mlp_oracle.MLPOracle([w.astype(np.float64) for w in Wl], bl, 3, 4, round_bf16=False)
+        o.W = [np.asarray(w, np.float64) for w in Wl]
+        o.b = [np.asarray(v, np.float64) for v in bl]
+        return o.loss_grad(x.astype(np.float64), count, hist)
+
+    loss, gW, gb = loss_of(W, b)
+    eps = 1e-6
+    for l in range(len(W)):
+        for (i, j) in [(0, 0), (1, 2), (W[l].shape[0] - 1, W[l].shape[1] - 1)]:
+            Wp = [w.copy() for w in W]
+            Wp[l][i, j] += eps
+            Wm = [w.copy() for w in W]
+            Wm[l][i, j] -= eps
+            num = (loss_of(Wp, b)[0] - loss_of(Wm, b)[0]) / (2 * eps)
+            assert gW[l][i, j] == pytest.approx(num, rel=1e-4, abs=1e-7)
+        bp = [v.copy() for v in b]
+        bp[l][0] += eps
+        bm = [v.copy() for v in b]
+        bm[l][0] -= eps
+        num = (loss_of(W, bp)[0] - loss_of(W, bm)[0]) / (2 * eps)
+        assert gb[l][0] == pytest.approx(num, rel=1e-4, abs=1e-7)
+
+
+def test_bf16_rounding_helper():
+    x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 65504.0], np.float32)
+    y = mlp_oracle.bf16(x)
+    assert y[0] == 1.0 and y[1] == 1.0  # tie to even
+    assert y[2] == np.float32(1.0078125)
+    assert abs(y[3] - -3.140625) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("M,N,K,a_trans,b_trans,k_split", [
+    (128, 256, 256, 0, 0, 0), (300, 80, 256, 0, 0, 0), (200, 16, 80, 0, 0, 0),
+    (256, 256, 1024, 1, 1, 4), (80, 256, 512, 1, 1, 2), (129, 64, 64, 0, 1, 0)])
+def test_tcgen05_gemm(pp, gpu_ctx, M, N, K, a_trans, b_trans, k_split):
+    torch = pytest.importorskip("torch")
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, generator=g).bfloat16()
+    B = torch.randn(N, K, generator=g).bfloat16()
+    a_dev = (A.t().contiguous() if a_trans else A).cuda()
+    b_dev = (B.t().contiguous() if b_trans else B).cuda()
+    lda = M if a_trans else K
+    ldb = N if b_trans else K
+    C = torch.zeros(M, N, dtype=torch.float32, device="cuda")
+    lib = pp._lib.load()
+    import ctypes
+    rc = lib.pp_mlp_gemm_test(ctypes.c_void_p(a_dev.data_ptr()), lda, a_trans,
+                              ctypes.c_void_p(b_dev.data_ptr()), ldb, b_trans, M, N, K, k_split,
+                              ctypes.c_void_p(C.data_ptr()), N, None)
+    assert rc == 0, pp._lib.last_error()
+    want = (A.float() @ B.float().t()).numpy()
+    got = C.cpu().numpy()
+    np.testing.assert_allclose(got, want, rtol=1e-3, atol=1e-3 * np.sqrt(K))
+
+
+def _make(pp, B, seed=0):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(B, 8)).astype(np.float32)
+    count = rng.poisson(5.0, B).astype(np.float32)
+    hist = rng.poisson(0.5, (B, 64)).astype(np.float32)
+    return x, count, hist, [torch.tensor(a, device="cuda") for a in (x, count, hist)]
+
+
+@pytest.mark.gpu
+def test_mlp_gradients_match_oracle(pp, gpu_ctx):
+    B = 1024
+    mlp = pp.surrogate.MLP(max_batch=B, seed=3)
+    x, count, hist, dev = _make(pp, B)
+    loss, g = mlp.loss_grad(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), B)
+    W, b = mlp.unpack(mlp.params())
+    o = mlp_oracle.MLPOracle(W, b, 8, 64)
+    loss_ref, gW, gb = o.loss_grad(x, count, hist)
+    assert loss == pytest.approx(loss_ref, rel=1e-3)
+    gW_dev, gb_dev = mlp.unpack(g)
+    for l in range(len(gW)):
+        for got, want, name in ((gW_dev[l], gW[l], "W"), (gb_dev[l], gb[l], "b")):
+            err = np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-12)
+            assert err < 2e-2, (l, name, err)
+    mlp.close()
+
+
+@pytest.mark.gpu
+def test_mlp_training_reduces_loss(pp, gpu_ctx):
+    torch = pytest.importorskip("torch")
+    B = 2048
+    rng = np.random.default_rng(1)
+    n = 16384
+    x = rng.normal(size=(n, 8)).astype(np.float32)
+    mu = np.exp(1.0 + 0.8 * x[:, 0] - 0.5 * x[:, 1] ** 2)
+    count = rng.poisson(mu).astype(np.float32)
+    centre = np.clip((20 + 10 * x[:, 2]).astype(int), 0, 63)
+    hist = np.zeros((n, 64), np.float32)
+    hist[np.arange(n), centre] = count
+    t = [torch.tensor(a, device="cuda") for a in (x, count, hist)]
+    mlp = pp.surrogate.MLP(max_batch=B, seed=4)
+    log = pp.surrogate.train(mlp, t[0], t[1], t[2], steps=300, batch=B, lr=1e-3, log_every=50)
+    first, last = log[0][1], log[-1][1]
+    assert np.isfinite(last) and last < 0.5 * first, log
+    mlp.close()
