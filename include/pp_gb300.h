@@ -349,6 +349,16 @@ PP_API int pp_mlp_loss_grad(pp_mlp* mlp, const float* d_x, const float* d_count,
 PP_API int pp_mlp_train_step(pp_mlp* mlp, const float* d_x, const float* d_count,
                              const float* d_hist, int32_t B, float lr, void* stream);
 PP_API int pp_mlp_last_loss(pp_mlp* mlp, float* host_loss);
+/* Fused inference (one tcgen05 kernel; activations stay in shared memory):
+ * d_x (n x n_in, FP32, device) -> d_expect[n] = exp(min(log-count, 30)) and,
+ * when d_pdf is not NULL, d_pdf (n x n_bins) = softmax of the time logits.
+ * Asynchronous on `stream`; n is not limited by max_batch.  Timeouts of the
+ * kernel's waits set a device flag that pp_mlp_check reports. */
+PP_API int pp_mlp_infer(pp_mlp* mlp, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
+                        void* stream);
+/* Synchronises `stream`; PP_ERR_TIMEOUT (and clears the flag) if a
+ * tensor-core wait of an earlier MLP kernel gave up. */
+PP_API int pp_mlp_check(pp_mlp* mlp, void* stream);
 /* One tcgen05 GEMM (test hook): C = A * B^T, BF16 in, FP32 out (k_split > 0:
  * C += over K slices). */
 PP_API int pp_mlp_gemm_test(const void* d_a, int64_t lda, int32_t a_trans, const void* d_b,

@@ -59,6 +59,15 @@ class MLPOracle:
         self.O = a @ W16[-1].T + self.b[-1]
         return self.O
 
+    def predict(self, x):
+        """Expected count exp(min(o0, 30)) and the softmax time PDF, the outputs
+        of the fused inference kernel."""
+        O = self.forward(x)
+        lam = np.exp(np.minimum(O[:, 0], 30.0))
+        logits = O[:, 1:1 + self.n_bins]
+        e = np.exp(logits - logits.max(axis=1, keepdims=True))
+        return lam, e / e.sum(axis=1, keepdims=True)
+
     def loss_grad(self, x, count, hist):
         r = self.r
         O = self.forward(x)

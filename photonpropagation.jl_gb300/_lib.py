@@ -162,6 +162,8 @@ SIGNATURES = {
     "pp_mlp_train_step": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_float,
                                     c_void_p]),
     "pp_mlp_last_loss": (c_int32, [c_void_p, POINTER(c_float)]),
+    "pp_mlp_infer": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "pp_mlp_check": (c_int32, [c_void_p, c_void_p]),
     "pp_mlp_gemm_test": (c_int32, [c_void_p, c_int64, c_int32, c_void_p, c_int64, c_int32,
                                    c_int32, c_int32, c_int32, c_int32, c_void_p, c_int64,
                                    c_void_p]),

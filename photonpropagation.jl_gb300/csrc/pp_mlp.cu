@@ -300,6 +300,192 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* _
   if (i < n) y[i] = __float2bfloat16(x[i]);
 }
 
+// Weights of layer l in the core-matrix layout the tensor core reads, so that
+// the fused kernel can copy a whole layer into shared memory with one TMA
+// bulk copy: element (r, c) of the rows x cols matrix at byte
+// core_offset(r, c / 8, cols) + (c % 8) * 2.
+__global__ void repack_kernel(const bf16* __restrict__ w, int rows, int cols,
+                              unsigned char* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)rows * cols) return;
+  const int r = (int)(i / cols), c = (int)(i % cols);
+  *reinterpret_cast<bf16*>(out + pptc::core_offset(r, c >> 3, cols) + (c & 7) * 2) = w[i];
+}
+
+constexpr int kMaxLayers = 17;
+struct InferParams {
+  const float* x;
+  long long n;
+  int n_in, in_pad, hidden, n_layers, out_pad, n_bins;
+  uint32_t tmem_cols;               // power of two >= 32 covering hidden and out_pad
+  const unsigned char* wpack;
+  long long wpack_off[kMaxLayers];  // bytes, multiples of 512
+  const float* P;                   // FP32 parameters (biases)
+  long long off_b[kMaxLayers];
+  float* expect;                    // [n]
+  float* pdf;                       // [n x n_bins], may be null
+  unsigned* err;
+};
+
+// The whole network for 128 rows in one CTA: the activations never leave
+// shared memory (core-matrix layout, the A operand of the next layer), each
+// layer's packed weights arrive by TMA bulk copies into a second buffer (the
+// B operand), the accumulator is 128 lanes x N columns of tensor memory.  The
+// head epilogue turns column 0 into the expected count exp(min(o, 30)) and
+// columns 1..n_bins into a softmax, staged through shared memory so that the
+// PDF rows are stored coalesced.
+__global__ void __launch_bounds__(128, 1) infer_kernel(const __grid_constant__ InferParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bar_mma;
+  __shared__ __align__(8) uint64_t bar_tma;
+  __shared__ uint32_t tmem_slot;
+  const int act_k = p.hidden > p.in_pad ? p.hidden : p.in_pad;
+  unsigned char* sA = smem;
+  unsigned char* sW = smem + (size_t)128 * act_k * 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long row0 = (long long)blockIdx.x * 128;
+  const int r = warp * 32 + lane;  // this thread's row in the tile = its TMEM lane
+  const long long row = row0 + r;
+  if (warp == 0) pptc::tmem_alloc(&tmem_slot, p.tmem_cols);
+  if (threadIdx.x == 0) {
+    pptc::mbar_init(&bar_mma, 1);
+    pptc::mbar_init(&bar_tma, 1);
+  }
+  for (int kb = 0; kb < p.in_pad / 8; ++kb) {
+    union {
+      uint4 u;
+      bf16 h[8];
+    } v;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = kb * 8 + j;
+      v.h[j] = __float2bfloat16(row < p.n && c < p.n_in ? p.x[row * p.n_in + c] : 0.0f);
+    }
+    *reinterpret_cast<uint4*>(sA + pptc::core_offset(r, kb, p.in_pad)) = v.u;
+  }
+  pptc::fence_before_sync();
+  __syncthreads();
+  pptc::fence_after_sync();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+  bool ok = true;
+  int kin = p.in_pad;
+  for (int l = 0; l <= p.n_layers; ++l) {
+    const bool head = l == p.n_layers;
+    const int rows = head ? p.out_pad : p.hidden;
+    const uint32_t wbytes = (uint32_t)rows * (uint32_t)kin * 2u;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                       pptc::smem_u32(&bar_tma)),
+                   "r"(wbytes)
+                   : "memory");
+      for (uint32_t off = 0; off < wbytes; off += 32768) {
+        const uint32_t nb = wbytes - off < 32768 ? wbytes - off : 32768;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+            "[%3];" ::"r"(pptc::smem_u32(sW + off)),
+            "l"(p.wpack + p.wpack_off[l] + off), "r"(nb), "r"(pptc::smem_u32(&bar_tma))
+            : "memory");
+      }
+    }
+    pptc::fence_async_smem();  // this thread's activation writes -> tensor-core reads
+    if (!__syncthreads_and(pptc::mbar_wait(&bar_tma, (uint32_t)(l & 1), kWaitNs))) {
+      // let the copies in flight land before the shared memory is released
+      pptc::mbar_wait(&bar_tma, (uint32_t)(l & 1), kWaitNs);
+      ok = false;
+      break;
+    }
+    if (threadIdx.x == 0) {
+      pptc::fence_after_sync();
+      const uint32_t sbo = (uint32_t)(kin / 8) * 128u;
+      const uint32_t idesc = pptc::idesc_bf16(128, rows);
+      for (int s = 0; s < kin / 16; ++s) {
+        const uint64_t ad = pptc::smem_desc(pptc::smem_u32(sA) + s * 256, 128, sbo);
+        const uint64_t bd = pptc::smem_desc(pptc::smem_u32(sW) + s * 256, 128, sbo);
+        pptc::mma_bf16(tmem, ad, bd, idesc, s > 0);
+      }
+      pptc::mma_commit(&bar_mma);
+    }
+    if (!__syncthreads_and(pptc::mbar_wait(&bar_mma, (uint32_t)(l & 1), kWaitNs))) {
+      pptc::mbar_wait(&bar_mma, (uint32_t)(l & 1), kWaitNs);
+      ok = false;
+      break;
+    }
+    pptc::fence_after_sync();
+    const float* bias = p.P + p.off_b[l];
+    if (!head) {
+      for (int c0 = 0; c0 < p.hidden; c0 += 32) {
+        float v[32];
+        pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (c0 + q * 8 >= p.hidden) break;
+          union {
+            uint4 u;
+            bf16 h[8];
+          } o;
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            o.h[j] = __float2bfloat16(pptc::silu(v[q * 8 + j] + bias[c0 + q * 8 + j]));
+          *reinterpret_cast<uint4*>(sA + pptc::core_offset(r, (c0 >> 3) + q, p.hidden)) = o.u;
+        }
+      }
+      kin = p.hidden;
+      pptc::fence_before_sync();
+      __syncthreads();
+      continue;
+    }
+    // head: pass 1 log count and softmax maximum, pass 2 the normaliser,
+    // pass 3 the probabilities into shared memory (all operands are consumed)
+    float o0 = 0.0f, mx = -INFINITY;
+    for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
+      float v[32];
+      pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const int c = c0 + i;
+        if (c == 0) o0 = v[i] + bias[0];
+        else if (c <= p.n_bins) mx = fmaxf(mx, v[i] + bias[c]);
+      }
+    }
+    float se = 0.0f;
+    for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
+      float v[32];
+      pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const int c = c0 + i;
+        if (c >= 1 && c <= p.n_bins) se += __expf(v[i] + bias[c] - mx);
+      }
+    }
+    if (row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
+    if (p.pdf) {
+      const float inv = 1.0f / se;
+      const int ld = p.n_bins + 1;  // odd stride: the 32 rows of a warp hit 32 banks
+      float* stage = reinterpret_cast<float*>(smem);
+      for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
+        float v[32];
+        pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int c = c0 + i;
+          if (c >= 1 && c <= p.n_bins) stage[r * ld + c - 1] = __expf(v[i] + bias[c] - mx) * inv;
+        }
+      }
+      __syncthreads();
+      const long long left = p.n - row0;
+      const int nrows = left < 128 ? (int)left : 128;
+      float* dst = p.pdf + row0 * p.n_bins;
+      for (int i = threadIdx.x; i < nrows * p.n_bins; i += 128)
+        dst[i] = stage[(i / p.n_bins) * ld + i % p.n_bins];
+    }
+  }
+  pptc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) pptc::tmem_dealloc(tmem, p.tmem_cols);
+  if (!ok && threadIdx.x == 0) atomicOr(p.err, 1u);
+}
+
 int fail(int code, const std::string& m) { return pp::report_error(code, m); }
 int cuda_fail(cudaError_t e, const char* what) {
   return fail(PP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -350,6 +536,9 @@ struct pp_mlp {
   bf16* dZ[2] = {nullptr, nullptr};
   float* loss = nullptr;
   unsigned* err = nullptr;
+  unsigned char* wpack = nullptr;       // BF16 weights in core-matrix layout
+  std::vector<long long> wpack_off;     // bytes per layer
+  bool pack_dirty = true;
   long long step = 0;
   float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f, time_weight = 1.0f;
 };
@@ -360,6 +549,7 @@ void mlp_free(pp_mlp* m) {
   cudaFree(m->P); cudaFree(m->G); cudaFree(m->Mo); cudaFree(m->Vo); cudaFree(m->P16);
   cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16); cudaFree(m->dO32);
   cudaFree(m->dZ[0]); cudaFree(m->dZ[1]); cudaFree(m->loss); cudaFree(m->err);
+  cudaFree(m->wpack);
   for (auto* p : m->Z) cudaFree(p);
   for (auto* p : m->Y) cudaFree(p);
 }
@@ -457,6 +647,25 @@ int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cu
   return PP_OK;
 }
 
+int mlp_repack(pp_mlp* m, cudaStream_t s) {
+  for (int l = 0; l <= m->n_layers; ++l) {
+    const long long n = (long long)m->rows[l] * m->cols[l];
+    repack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m->P16 + m->off_w[l], m->rows[l],
+                                                            m->cols[l], m->wpack + m->wpack_off[l]);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "repack weights");
+  m->pack_dirty = false;
+  return PP_OK;
+}
+
+size_t infer_smem_bytes(const pp_mlp* m) {
+  size_t w = 0;
+  for (int l = 0; l <= m->n_layers; ++l) w = std::max(w, (size_t)m->rows[l] * m->cols[l] * 2);
+  const size_t act = (size_t)128 * std::max(m->hidden, m->in_pad) * 2;
+  return std::max(act + w, (size_t)128 * (m->n_bins + 1) * 4);
+}
+
 int check_err(pp_mlp* m, cudaStream_t s) {
   unsigned h = 0;
   cudaError_t e = cudaMemcpyAsync(&h, m->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
@@ -545,6 +754,12 @@ PP_API int pp_mlp_create(pp_mlp** out, int32_t device, int32_t n_in, int32_t hid
   A((void**)&m->dZ[1], sizeof(bf16) * Bn * hidden);
   A((void**)&m->loss, sizeof(float));
   A((void**)&m->err, sizeof(unsigned));
+  long long wbytes = 0;
+  for (int l = 0; l <= n_layers; ++l) {
+    m->wpack_off.push_back(wbytes);
+    wbytes += (long long)m->rows[l] * m->cols[l] * 2;  // rows, cols multiples of 16: 512-byte steps
+  }
+  A((void**)&m->wpack, (size_t)wbytes);
   if (e == cudaSuccess) e = cudaMemcpy(m->P, h.data(), pb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->Mo, 0, pb);
   if (e == cudaSuccess) e = cudaMemset(m->Vo, 0, pb);
@@ -604,6 +819,7 @@ PP_API int pp_mlp_set_params(pp_mlp* m, const float* host, int64_t n) {
     to_bf16_kernel<<<(unsigned)((n + 255) / 256), 256>>>(m->P, n, m->P16);
     e = cudaDeviceSynchronize();
   }
+  m->pack_dirty = true;
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "pp_mlp_set_params");
 }
 
@@ -657,8 +873,51 @@ PP_API int pp_mlp_train_step(pp_mlp* m, const float* d_x, const float* d_count,
   const float bc2 = 1.0f - std::pow(m->b2, (float)m->step);
   adam_kernel<<<(unsigned)((m->n_params + 255) / 256), 256, 0, s>>>(
       m->P, m->G, m->Mo, m->Vo, m->n_params, lr, m->b1, m->b2, m->eps, bc1, bc2, m->P16);
+  m->pack_dirty = true;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "adam");
+}
+
+// Fused inference: expected count (exp of the clamped log-count output) and
+// the softmax time PDF of n feature rows, one CTA per 128 rows; n is not
+// limited by max_batch.  d_pdf may be null.
+PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
+                        void* stream) {
+  if (!m || !d_x || !d_expect || n < 0) return fail(PP_ERR_INVALID, "bad arguments");
+  if (m->n_layers + 1 > kMaxLayers) return fail(PP_ERR_INVALID, "too many layers");
+  if (n == 0) return PP_OK;
+  if ((n + 127) / 128 > 0x7FFFFFFFLL) return fail(PP_ERR_INVALID, "n too large");
+  cudaSetDevice(m->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (m->pack_dirty) {
+    int rc = mlp_repack(m, s);
+    if (rc != PP_OK) return rc;
+  }
+  const size_t smem = infer_smem_bytes(m);
+  cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return cuda_fail(e, "infer smem");
+  InferParams p{};
+  p.x = d_x; p.n = n; p.n_in = m->n_in; p.in_pad = m->in_pad; p.hidden = m->hidden;
+  p.n_layers = m->n_layers; p.out_pad = m->out_pad; p.n_bins = m->n_bins;
+  p.tmem_cols = 32;
+  while (p.tmem_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.tmem_cols *= 2;
+  p.wpack = m->wpack; p.P = m->P;
+  for (int l = 0; l <= m->n_layers; ++l) {
+    p.wpack_off[l] = m->wpack_off[l];
+    p.off_b[l] = m->off_b[l];
+  }
+  p.expect = d_expect; p.pdf = d_pdf; p.err = m->err;
+  infer_kernel<<<(unsigned)((n + 127) / 128), 128, smem, s>>>(p);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? PP_OK : cuda_fail(e, "infer kernel");
+}
+
+// Device error flag of the tensor-core kernels (timeouts), checked and cleared.
+PP_API int pp_mlp_check(pp_mlp* m, void* stream) {
+  if (!m) return fail(PP_ERR_INVALID, "null argument");
+  cudaSetDevice(m->device);
+  return check_err(m, (cudaStream_t)stream);
 }
 
 PP_API int pp_mlp_last_loss(pp_mlp* m, float* host_loss) {

@@ -84,51 +84,74 @@ def in_training_range(p: Pairs) -> np.ndarray:
     return (p.distance >= D_MIN) & (p.distance <= D_MAX) & (p.spectrum_id == 0)
 
 
+def source_positions(p: Pairs) -> np.ndarray:
+    """Cascade vertex of each pair with the module at the origin."""
+    return -p.distance[:, None] * p.module_dir
+
+
+def geometric_time(p: Pairs, medium=None) -> np.ndarray:
+    """(d - r) / v_group(800 nm), the direct-light time of the reference's
+    calc_tgeo (src/calc.jl) for a module of radius MODULE_RADIUS."""
+    medium = medium or CascadiaMediumProperties()
+    return (p.distance - MODULE_RADIUS) / float(medium.group_velocity(800.0))
+
+
+def table_setup(pairs: Pairs, photons: int, seed: int, medium=None, spectrum=None):
+    """One PhotonPropSetup holding every pair: the module at the origin and one
+    ExtendedCherenkovEmitter per pair (source index = pair index)."""
+    from .propsetup import PhotonPropSetup
+    medium = medium or CascadiaMediumProperties()
+    spectrum = spectrum or make_cherenkov_spectrum((300.0, 800.0), medium)
+    pos = source_positions(pairs)
+    srcs = [ExtendedCherenkovEmitter(pos[i], pairs.emitter_dir[i], 0.0, photons, CASCADE)
+            for i in range(len(pairs))]
+    tgt = HomogeneousDetector(Spherical([0.0, 0.0, 0.0], MODULE_RADIUS), 1.0, 1)
+    return PhotonPropSetup(srcs, [tgt], medium, spectrum, seed)
+
+
 def generate_tables(pairs: Pairs, photons: int, seed: int = 1, ctx=None, medium=None,
-                    spectrum=None, device: int = 0, chunk: int = 262144, n_steps: int = 15):
+                    spectrum=None, device: int = 0, chunk: int = 262144, n_steps: int = 15,
+                    device_out: bool = False):
     """Expected hits and time histograms of every pair (one MC run each).
 
     The module sits at the origin; pair i is a cascade at -d_i * module_dir_i
     pointing along emitter_dir_i, so all pairs share one target and run in one
-    persistent launch per chunk.  Returns (counts [n], hists [n x 64]) as numpy
-    arrays for `photons` photons per pair."""
+    persistent launch per chunk of pairs (chunk k uses seed + k * chunk).
+    Returns (counts [n], hists [n x 64]) for `photons` photons per pair, as
+    numpy arrays or, with device_out, as CUDA tensors."""
     import torch
     from .context import Context
     medium = medium or CascadiaMediumProperties()
     spectrum = spectrum or make_cherenkov_spectrum((300.0, 800.0), medium)
     own = ctx is None
     ctx = ctx or Context(device)
-    from .propsetup import PhotonPropSetup
-    tgt = HomogeneousDetector(Spherical([0.0, 0.0, 0.0], MODULE_RADIUS), 1.0, 1)
-    base = PhotonPropSetup([ExtendedCherenkovEmitter([0, 0, -10], [0, 0, 1], 0.0, 1, CASCADE)],
-                           [tgt], medium, spectrum, seed)
-    base.upload(ctx)
-    v800 = float(medium.group_velocity(800.0))
     n = len(pairs)
-    counts = np.zeros(n, np.float32)
-    hists = np.zeros((n, N_BINS), np.float32)
+    counts = torch.empty(n, dtype=torch.float32, device="cuda")
+    hists = torch.empty((n, N_BINS), dtype=torch.float32, device="cuda")
     ctr = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    tgeo_all = torch.tensor(geometric_time(pairs, medium), dtype=torch.float32, device="cuda")
+    first = True
     for lo in range(0, n, chunk):
         hi = min(n, lo + chunk)
-        sub = pairs.subset(slice(lo, hi))
-        pos = -sub.distance[:, None] * sub.module_dir
-        srcs = [ExtendedCherenkovEmitter(pos[i], sub.emitter_dir[i], 0.0, photons, CASCADE)
-                for i in range(hi - lo)]
-        recs = to_records(srcs)
-        ctx.set_sources(recs, hi - lo, 1.0)
-        tgeo = torch.tensor((sub.distance - MODULE_RADIUS) / v800, dtype=torch.float32,
-                            device="cuda")
+        setup = table_setup(pairs.subset(slice(lo, hi)), photons, seed + lo, medium, spectrum)
+        if first:
+            setup.upload(ctx)
+            first = False
+        ctx.set_sources(setup.source_records(), hi - lo, 1.0)
         hist = torch.empty((hi - lo, N_BINS + 1), dtype=torch.float32, device="cuda")
-        check(ctx._lib.pp_launch_histogram(ctx.ptr, seed + lo, n_steps, c_void_p(tgeo.data_ptr()),
+        check(ctx._lib.pp_launch_histogram(ctx.ptr, seed + lo, n_steps,
+                                           c_void_p(tgeo_all[lo:hi].data_ptr()),
                                            c_void_p(hist.data_ptr()), N_BINS, T_OFFSET, LOG_T_LO,
                                            LOG_T_HI, c_void_p(ctr.data_ptr()), None),
               "pp_launch_histogram")
-        h = hist.cpu().numpy()
-        counts[lo:hi] = h[:, 0]
-        hists[lo:hi] = h[:, 1:]
+        counts[lo:hi] = hist[:, 0]
+        hists[lo:hi] = hist[:, 1:]
+    torch.cuda.synchronize()
     if own:
         ctx.close()
-    return counts, hists
+    if device_out:
+        return counts, hists
+    return counts.cpu().numpy(), hists.cpu().numpy()
 
 
 class MLP:
@@ -185,6 +208,14 @@ class MLP:
     def forward(self, x_dev, B, out_dev, stream=0):
         check(self._lib.pp_mlp_forward(self.ptr, c_void_p(x_dev), B, c_void_p(out_dev),
                                        c_void_p(stream)), "pp_mlp_forward")
+
+    def infer(self, x_dev, n, expect_dev, pdf_dev=0, stream=0, check_now=True):
+        """Fused tcgen05 inference of n rows (device pointers): expected counts
+        and, when pdf_dev is given, the time PDFs (n x n_bins)."""
+        check(self._lib.pp_mlp_infer(self.ptr, c_void_p(x_dev), int(n), c_void_p(expect_dev),
+                                     c_void_p(pdf_dev or None), c_void_p(stream)), "pp_mlp_infer")
+        if check_now:
+            check(self._lib.pp_mlp_check(self.ptr, c_void_p(stream)), "pp_mlp_infer")
 
     def loss_grad(self, x_dev, count_dev, hist_dev, B):
         g = np.empty(self.n_params, np.float32)

@@ -131,3 +131,55 @@ def test_mlp_training_reduces_loss(pp, gpu_ctx):
     first, last = log[0][1], log[-1][1]
     assert np.isfinite(last) and last < 0.5 * first, log
     mlp.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,hidden,layers,n_bins", [
+    (1000, 256, 4, 64), (129, 48, 2, 20), (128, 256, 1, 255), (5, 64, 3, 64)])
+def test_fused_inference_matches_oracle(pp, gpu_ctx, n, hidden, layers, n_bins):
+    torch = pytest.importorskip("torch")
+    mlp = pp.surrogate.MLP(max_batch=256, hidden=hidden, n_layers=layers, n_bins=n_bins, seed=5)
+    rng = np.random.default_rng(n)
+    # trained-looking scale: random weights with a non-trivial time head
+    flat = mlp.params()
+    W, b = mlp.unpack(flat)
+    for l in range(len(W)):
+        b[l][:] = rng.normal(0, 0.2, b[l].shape)
+    W[-1][1:] *= 3.0
+    mlp.set_params(flat)
+    x = rng.normal(size=(n, 8)).astype(np.float32)
+    xd = torch.tensor(x, device="cuda")
+    expect = torch.full((n,), -1.0, device="cuda")
+    pdf = torch.full((n, n_bins), -1.0, device="cuda")
+    mlp.infer(xd.data_ptr(), n, expect.data_ptr(), pdf.data_ptr())
+    W, b = mlp.unpack(mlp.params())
+    lam, p_ref = mlp_oracle.MLPOracle(W, b, 8, n_bins).predict(x)
+    got_l, got_p = expect.cpu().numpy(), pdf.cpu().numpy()
+    # BF16 activations: one rounding flip moves an output by ~1e-3
+    np.testing.assert_allclose(got_l, lam, rtol=5e-3)
+    np.testing.assert_allclose(got_p.sum(axis=1), 1.0, rtol=1e-5)
+    np.testing.assert_allclose(got_p, p_ref, rtol=1e-2, atol=1e-5)
+    # the expected counts alone (no PDF output)
+    e2 = torch.zeros(n, device="cuda")
+    mlp.infer(xd.data_ptr(), n, e2.data_ptr())
+    assert torch.equal(e2, expect)
+    mlp.close()
+
+
+@pytest.mark.gpu
+def test_fused_inference_follows_training(pp, gpu_ctx):
+    """The packed inference weights are refreshed after each Adam step."""
+    torch = pytest.importorskip("torch")
+    B = 512
+    x, count, hist, dev = _make(pp, B, seed=2)
+    mlp = pp.surrogate.MLP(max_batch=B, seed=6)
+    e0 = torch.zeros(B, device="cuda")
+    mlp.infer(dev[0].data_ptr(), B, e0.data_ptr())
+    mlp.train_step(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), B, 1e-2)
+    e1 = torch.zeros(B, device="cuda")
+    mlp.infer(dev[0].data_ptr(), B, e1.data_ptr())
+    assert not torch.equal(e0, e1)
+    W, b = mlp.unpack(mlp.params())
+    lam, _ = mlp_oracle.MLPOracle(W, b, 8, 64).predict(x)
+    np.testing.assert_allclose(e1.cpu().numpy(), lam, rtol=5e-3)
+    mlp.close()
