@@ -349,6 +349,12 @@ PP_API int pp_mlp_loss_grad(pp_mlp* mlp, const float* d_x, const float* d_count,
 PP_API int pp_mlp_train_step(pp_mlp* mlp, const float* d_x, const float* d_count,
                              const float* d_hist, int32_t B, float lr, void* stream);
 PP_API int pp_mlp_last_loss(pp_mlp* mlp, float* host_loss);
+/* Adam moments (n = pp_mlp_num_params floats each; NULL skips one on get)
+ * and step count, for training checkpoints. */
+PP_API int pp_mlp_get_adam(const pp_mlp* mlp, float* host_m, float* host_v, int64_t n,
+                           int64_t* step);
+PP_API int pp_mlp_set_adam(pp_mlp* mlp, const float* host_m, const float* host_v, int64_t n,
+                           int64_t step);
 /* Fused inference (one tcgen05 kernel; activations stay in shared memory):
  * d_x (n x n_in, FP32, device) -> d_expect[n] = exp(min(log-count, 30)) and,
  * when d_pdf is not NULL, d_pdf (n x n_bins) = softmax of the time logits.

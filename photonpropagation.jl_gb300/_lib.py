@@ -164,6 +164,10 @@ SIGNATURES = {
     "pp_mlp_last_loss": (c_int32, [c_void_p, POINTER(c_float)]),
     "pp_mlp_infer": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "pp_mlp_check": (c_int32, [c_void_p, c_void_p]),
+    "pp_mlp_get_adam": (c_int32, [c_void_p, POINTER(c_float), POINTER(c_float), c_int64,
+                                  POINTER(c_int64)]),
+    "pp_mlp_set_adam": (c_int32, [c_void_p, POINTER(c_float), POINTER(c_float), c_int64,
+                                  c_int64]),
     "pp_mlp_gemm_test": (c_int32, [c_void_p, c_int64, c_int32, c_void_p, c_int64, c_int32,
                                    c_int32, c_int32, c_int32, c_int32, c_void_p, c_int64,
                                    c_void_p]),

@@ -878,6 +878,32 @@ PP_API int pp_mlp_train_step(pp_mlp* m, const float* d_x, const float* d_count,
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "adam");
 }
 
+// Adam state for checkpoints: first and second moments (n floats each, either
+// may be null) and the step count.
+PP_API int pp_mlp_get_adam(const pp_mlp* m, float* host_m, float* host_v, int64_t n,
+                           int64_t* step) {
+  if (!m || n != m->n_params) return fail(PP_ERR_INVALID, "bad moment buffers");
+  cudaSetDevice(m->device);
+  cudaError_t e = cudaSuccess;
+  if (host_m) e = cudaMemcpy(host_m, m->Mo, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && host_v)
+    e = cudaMemcpy(host_v, m->Vo, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  if (step) *step = m->step;
+  return e == cudaSuccess ? PP_OK : cuda_fail(e, "pp_mlp_get_adam");
+}
+
+PP_API int pp_mlp_set_adam(pp_mlp* m, const float* host_m, const float* host_v, int64_t n,
+                           int64_t step) {
+  if (!m || !host_m || !host_v || n != m->n_params || step < 0)
+    return fail(PP_ERR_INVALID, "bad moment buffers");
+  cudaSetDevice(m->device);
+  cudaError_t e = cudaMemcpy(m->Mo, host_m, sizeof(float) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->Vo, host_v, sizeof(float) * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "pp_mlp_set_adam");
+  m->step = step;
+  return PP_OK;
+}
+
 // Fused inference: expected count (exp of the clamped log-count output) and
 // the softmax time PDF of n feature rows, one CTA per 128 rows; n is not
 // limited by max_batch.  d_pdf may be null.

@@ -231,6 +231,31 @@ class MLP:
                                           c_void_p(hist_dev), B, float(lr), c_void_p(stream)),
               "pp_mlp_train_step")
 
+    def save(self, path: str) -> None:
+        """Checkpoint: shape, parameters and Adam state in one .npz file."""
+        m = np.empty(self.n_params, np.float32)
+        v = np.empty(self.n_params, np.float32)
+        st = c_int64()
+        fp = ctypes.POINTER(c_float)
+        check(self._lib.pp_mlp_get_adam(self.ptr, m.ctypes.data_as(fp), v.ctypes.data_as(fp),
+                                        self.n_params, byref(st)), "pp_mlp_get_adam")
+        np.savez(path, shape=np.array([self.n_in, self.hidden, self.n_layers, self.n_bins]),
+                 params=self.params(), adam_m=m, adam_v=v, step=np.array([st.value]))
+
+    @classmethod
+    def load(cls, path: str, device=0, max_batch=8192):
+        z = np.load(path)
+        n_in, hidden, n_layers, n_bins = (int(v) for v in z["shape"])
+        net = cls(device=device, n_in=n_in, hidden=hidden, n_layers=n_layers, n_bins=n_bins,
+                  max_batch=max_batch)
+        net.set_params(z["params"])
+        fp = ctypes.POINTER(c_float)
+        m = np.ascontiguousarray(z["adam_m"], np.float32)
+        v = np.ascontiguousarray(z["adam_v"], np.float32)
+        check(net._lib.pp_mlp_set_adam(net.ptr, m.ctypes.data_as(fp), v.ctypes.data_as(fp),
+                                       net.n_params, int(z["step"][0])), "pp_mlp_set_adam")
+        return net
+
     def last_loss(self) -> float:
         v = c_float()
         check(self._lib.pp_mlp_last_loss(self.ptr, byref(v)), "pp_mlp_last_loss")
@@ -258,3 +283,144 @@ def train(mlp: MLP, x, counts, hists, steps: int, batch: int = 8192, lr: float =
         if log_every and (s % log_every == 0 or s == steps - 1):
             log.append((s, mlp.last_loss()))
     return log
+
+
+# ---------------------------------------------------------------------------
+# Serving: the network answers, the plain MC is fallback and judge.
+
+def analytic_expectation(p: Pairs, photons: float, att_len: float = 25.0,
+                         norm: float = 1.0) -> np.ndarray:
+    """The reference's closed-form distance scaling of a module's photon
+    count, norm * N * r^2 / (4 d^2) * exp(-d / att_len)
+    (examples/validation.jl:307-312): the method without a surrogate."""
+    return norm * photons * MODULE_RADIUS ** 2 / (4.0 * p.distance ** 2) * np.exp(
+        -p.distance / att_len)
+
+
+def fit_analytic_norm(p: Pairs, counts: np.ndarray, photons: float, att_len: float = 25.0):
+    """Least-squares norm of analytic_expectation to MC counts (the
+    curve_fit of examples/validation.jl:314)."""
+    a = analytic_expectation(p, photons, att_len)
+    return float(np.sum(a * counts) / max(np.sum(a * a), 1e-300))
+
+
+def ks_distance(pdf: np.ndarray, hist: np.ndarray) -> np.ndarray:
+    """Row-wise Kolmogorov-Smirnov distance between binned PDFs and histograms."""
+    c1 = np.cumsum(pdf, axis=1)
+    c1 = c1 / np.maximum(c1[:, -1:], 1e-30)
+    c2 = np.cumsum(hist, axis=1)
+    c2 = c2 / np.maximum(c2[:, -1:], 1e-30)
+    return np.abs(c1 - c2).max(axis=1)
+
+
+@dataclass
+class Expectations:
+    counts: np.ndarray          # expected hits for the requested photons per pair
+    pdf: np.ndarray | None      # n x N_BINS arrival-time PDFs (None if not requested;
+                                # NaN rows: answered by an MC run that saw no hit)
+    from_mc: np.ndarray         # bool: answered by the MC (outside range, audited, failed)
+    audit: dict                 # audit statistics of this batch
+
+
+class Surrogate:
+    """Module expectations from the trained network, with the plain MC as
+    fallback and judge.
+
+    Pairs outside the training ranges, and a random `audit_fraction` of the
+    rest, run through the MC at `fallback_photons` per pair.  The audited
+    pairs measure the network's error on this batch: relative count error
+    where the MC saw at least `min_audit_hits` (so that its own Poisson error
+    is small) and the KS distance of the time PDFs.  If the median count
+    error exceeds `max_median_error`, the batch fails its error check and,
+    with on_failure="mc", every pair of the batch is answered by the MC."""
+
+    def __init__(self, mlp: MLP, table_photons: float = 1e5, ctx=None,
+                 fallback_photons: int = 10_000_000, audit_fraction: float = 0.01,
+                 min_audit_hits: float = 400.0, max_median_error: float = 0.05,
+                 on_failure: str = "mc", medium=None, spectrum=None):
+        if on_failure not in ("mc", "flag"):
+            raise ValueError("on_failure must be 'mc' or 'flag'")
+        self.mlp = mlp
+        self.table_photons = float(table_photons)
+        self.ctx = ctx
+        self.fallback_photons = int(fallback_photons)
+        self.audit_fraction = float(audit_fraction)
+        self.min_audit_hits = float(min_audit_hits)
+        self.max_median_error = float(max_median_error)
+        self.on_failure = on_failure
+        self.medium = medium
+        self.spectrum = spectrum
+
+    def infer(self, p: Pairs, with_pdf: bool = True):
+        """Network outputs for every pair (device tensors: counts per
+        table_photons, PDFs or None)."""
+        import torch
+        n = len(p)
+        x = torch.tensor(pair_features(p), device="cuda")
+        counts = torch.empty(n, dtype=torch.float32, device="cuda")
+        pdf = torch.empty((n, N_BINS), dtype=torch.float32, device="cuda") if with_pdf else None
+        self.mlp.infer(x.data_ptr(), n, counts.data_ptr(), pdf.data_ptr() if with_pdf else 0)
+        return counts, pdf
+
+    @staticmethod
+    def _normalise(h):
+        """Histograms to PDFs; rows without any MC hit have no PDF (NaN)."""
+        tot = h.sum(axis=1, keepdims=True)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return np.where(tot > 0, h / tot, np.nan)
+
+    def _mc(self, p: Pairs, seed: int):
+        if self.spectrum is None and np.any(p.spectrum_id != 0):
+            raise ValueError("only spectrum id 0 (Frank-Tamm, 300-800 nm) has a default table")
+        c, h = generate_tables(p, self.fallback_photons, seed=seed, ctx=self.ctx,
+                               medium=self.medium, spectrum=self.spectrum)
+        return c.astype(np.float64), h
+
+    def expectations(self, p: Pairs, photons: float | None = None, seed: int = 0,
+                     with_pdf: bool = True) -> Expectations:
+        photons = self.table_photons if photons is None else float(photons)
+        n = len(p)
+        counts_d, pdf_d = self.infer(p, with_pdf)
+        counts = counts_d.cpu().numpy().astype(np.float64) * (photons / self.table_photons)
+        pdf = pdf_d.cpu().numpy() if with_pdf else None
+        rng = np.random.default_rng(seed)
+        inside = in_training_range(p)
+        audit = np.flatnonzero(inside & (rng.random(n) < self.audit_fraction))
+        mc_idx = np.union1d(np.flatnonzero(~inside), audit)
+        from_mc = np.zeros(n, bool)
+        stats = {"n_pairs": n, "n_outside": int((~inside).sum()), "n_audited": int(audit.size)}
+        if mc_idx.size:
+            mc_c, mc_h = self._mc(p.subset(mc_idx), seed)
+            scale = photons / self.fallback_photons
+            pos = np.searchsorted(mc_idx, audit)
+            judged = mc_c[pos] >= self.min_audit_hits
+            nn_a = counts[audit] / scale
+            rel = np.abs(nn_a[judged] - mc_c[pos][judged]) / mc_c[pos][judged]
+            stats.update({
+                "n_judged": int(judged.sum()),
+                "median_rel_error": float(np.median(rel)) if rel.size else float("nan"),
+                "p95_rel_error": float(np.quantile(rel, 0.95)) if rel.size else float("nan"),
+                # the part of the error that is the judge's own Poisson noise
+                "judge_noise_median": float(np.median(0.6745 / np.sqrt(mc_c[pos][judged])))
+                if rel.size else float("nan"),
+            })
+            if with_pdf and rel.size:
+                ks = ks_distance(pdf[audit][judged], mc_h[pos][judged])
+                stats.update({"median_ks": float(np.median(ks)),
+                              "p95_ks": float(np.quantile(ks, 0.95))})
+            counts[mc_idx] = mc_c * scale
+            if with_pdf:
+                pdf[mc_idx] = self._normalise(mc_h)
+            from_mc[mc_idx] = True
+        # no audited pair with enough MC statistics: no evidence against the network
+        failed = bool(stats.get("median_rel_error", 0.0) > self.max_median_error)
+        stats["passed"] = not failed
+        if failed and self.on_failure == "mc":
+            rest = np.flatnonzero(~from_mc)
+            if rest.size:
+                mc_c, mc_h = self._mc(p.subset(rest), seed + 1)
+                counts[rest] = mc_c * (photons / self.fallback_photons)
+                if with_pdf:
+                    pdf[rest] = self._normalise(mc_h)
+                from_mc[rest] = True
+        return Expectations(counts, pdf, from_mc, stats)

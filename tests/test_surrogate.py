@@ -86,3 +86,137 @@ def test_histogram_tables_match_oracle(pp, orc, gpu_ctx):
     np.testing.assert_allclose(hists.sum(axis=1), counts, rtol=1e-4, atol=1e-3)
     l1 = np.abs(hists - want_h).sum()
     assert l1 <= 2.0 + 1e-3 * want_h.sum(), l1
+
+
+TABLE_PHOTONS = 100_000
+
+
+@pytest.fixture(scope="module")
+def trained(pp, gpu_ctx):
+    """A network trained on 1e5 MC tables (1e5 photons each), the way the
+    full-size training runs, only smaller."""
+    torch = pytest.importorskip("torch")
+    s = pp.surrogate
+    ctx = pp.get_context(0)
+    pairs = s.sample_pairs(100_000, seed=21)
+    c, h = s.generate_tables(pairs, TABLE_PHOTONS, seed=21, ctx=ctx, device_out=True)
+    x = torch.tensor(s.pair_features(pairs), device="cuda")
+    mlp = s.MLP(max_batch=8192, seed=1)
+    log = s.train(mlp, x, c, h, steps=2500, batch=8192, lr=1e-3, log_every=500)
+    assert np.isfinite(log[-1][1]) and log[-1][1] < log[0][1]
+    yield mlp
+    mlp.close()
+
+
+@pytest.mark.gpu
+def test_surrogate_gain_over_the_methods_without_it(pp, gpu_ctx, trained):
+    """Against a 1e7-photon MC judge, the trained network's counts beat both
+    the reference's analytic distance scaling and an MC run of the same cost
+    as one training table entry; its time PDFs are close in KS distance; and
+    it answers far faster than the MC."""
+    import time
+    s = pp.surrogate
+    ctx = pp.get_context(0)
+    ev = s.sample_pairs(300, seed=77)
+    judge_ph = 10_000_000
+    t0 = time.perf_counter()
+    jc, jh = s.generate_tables(ev, judge_ph, seed=5, ctx=ctx)
+    mc_rate = len(ev) / (time.perf_counter() - t0)
+    lc, _ = s.generate_tables(ev, TABLE_PHOTONS, seed=6, ctx=ctx)
+    sur = s.Surrogate(trained, table_photons=TABLE_PHOTONS, ctx=ctx)
+    nn_d, pdf_d = sur.infer(ev)
+    nn = nn_d.cpu().numpy() * (judge_ph / TABLE_PHOTONS)
+    ok = jc >= 400
+    assert ok.sum() >= 10
+    rel_nn = np.abs(nn - jc)[ok] / jc[ok]
+    rel_mc = np.abs(lc * (judge_ph / TABLE_PHOTONS) - jc)[ok] / jc[ok]
+    norm = s.fit_analytic_norm(ev.subset(ok), jc[ok], judge_ph)
+    rel_an = np.abs(s.analytic_expectation(ev, judge_ph, norm=norm) - jc)[ok] / jc[ok]
+    med = {k: float(np.median(v)) for k, v in (("nn", rel_nn), ("mc", rel_mc), ("an", rel_an))}
+    assert med["nn"] < 0.08, med
+    assert med["nn"] < 0.5 * med["mc"] and med["nn"] < 0.25 * med["an"], med
+    ks = s.ks_distance(pdf_d.cpu().numpy()[ok], jh[ok])
+    assert np.median(ks) < 0.06, np.median(ks)
+    # throughput: one inference launch over 1e5 pairs vs the MC's pairs/s
+    import torch
+    big = s.sample_pairs(100_000, seed=3)
+    x = torch.tensor(s.pair_features(big), device="cuda")
+    out = torch.empty(len(big), device="cuda")
+    trained.infer(x.data_ptr(), len(big), out.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    trained.infer(x.data_ptr(), len(big), out.data_ptr())
+    nn_rate = len(big) / (time.perf_counter() - t0)
+    assert nn_rate > 100 * mc_rate, (nn_rate, mc_rate)
+
+
+@pytest.mark.gpu
+def test_surrogate_fallback_and_audit(pp, gpu_ctx, trained):
+    s = pp.surrogate
+    ctx = pp.get_context(0)
+    ev = s.sample_pairs(400, seed=31)
+    ev.distance[:5] = [2.0, 3.0, 4.5, 320.0, 500.0]  # outside the training range
+    # a loose error bound: this test is about the mechanics, with few judged pairs
+    sur = s.Surrogate(trained, table_photons=TABLE_PHOTONS, ctx=ctx, audit_fraction=0.1,
+                      max_median_error=0.2)
+    r = sur.expectations(ev, photons=1e6, seed=4)
+    assert r.audit["n_outside"] == 5 and r.from_mc[:5].all()
+    assert 15 <= r.audit["n_audited"] <= 70 and r.from_mc.sum() == 5 + r.audit["n_audited"]
+    assert r.audit["passed"], r.audit
+    # MC answers (1e7 photons) are scaled to the requested photons
+    mc_c, _ = s.generate_tables(ev.subset(np.flatnonzero(r.from_mc)), 10_000_000, seed=4,
+                                ctx=ctx)
+    np.testing.assert_allclose(r.counts[r.from_mc], mc_c * 0.1, rtol=1e-5)
+    seen = r.counts > 0
+    np.testing.assert_allclose(r.pdf[seen].sum(axis=1), 1.0, rtol=1e-4)
+    assert np.isnan(r.pdf[~seen]).all() and r.from_mc[~seen].all()
+    # network answers scale with the requested photons
+    r2 = sur.expectations(ev, photons=2e6, seed=4, with_pdf=False)
+    nn = ~r.from_mc
+    np.testing.assert_allclose(r2.counts[nn], 2 * r.counts[nn], rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_surrogate_failed_audit_falls_back_to_mc(pp, gpu_ctx):
+    """An untrained network fails the audit's error check: the whole batch is
+    then answered by the MC."""
+    s = pp.surrogate
+    ctx = pp.get_context(0)
+    mlp = s.MLP(max_batch=256, seed=9)
+    ev = s.sample_pairs(60, seed=5)
+    ev.distance[:] = np.linspace(5.0, 7.0, 60)
+    sur = s.Surrogate(mlp, ctx=ctx, fallback_photons=1_000_000, audit_fraction=0.3,
+                      min_audit_hits=50)
+    r = sur.expectations(ev, seed=2)
+    assert not r.audit["passed"] and r.from_mc.all()
+    flagged = s.Surrogate(mlp, ctx=ctx, fallback_photons=1_000_000, audit_fraction=0.3,
+                          min_audit_hits=50, on_failure="flag").expectations(ev, seed=2)
+    assert not flagged.audit["passed"] and not flagged.from_mc.all()
+    mlp.close()
+
+
+@pytest.mark.gpu
+def test_training_checkpoint_resume(pp, gpu_ctx, tmp_path):
+    """Parameters and Adam state saved mid-run: resuming from the file
+    continues the same trajectory as the uninterrupted run."""
+    torch = pytest.importorskip("torch")
+    s = pp.surrogate
+    rng = np.random.default_rng(3)
+    B = 1024
+    x = torch.tensor(rng.normal(size=(B, 8)).astype(np.float32), device="cuda")
+    c = torch.tensor(rng.poisson(4.0, B).astype(np.float32), device="cuda")
+    h = torch.tensor(rng.poisson(0.3, (B, 64)).astype(np.float32), device="cuda")
+    a = s.MLP(max_batch=B, seed=2)
+    for _ in range(5):
+        a.train_step(x.data_ptr(), c.data_ptr(), h.data_ptr(), B, 1e-3)
+    path = str(tmp_path / "ckpt.npz")
+    a.save(path)
+    b = s.MLP.load(path, max_batch=B)
+    np.testing.assert_array_equal(a.params(), b.params())
+    for net in (a, b):
+        for _ in range(5):
+            net.train_step(x.data_ptr(), c.data_ptr(), h.data_ptr(), B, 1e-3)
+    pa, pb = a.params(), b.params()
+    assert np.linalg.norm(pa - pb) <= 1e-3 * np.linalg.norm(pa)
+    a.close()
+    b.close()
