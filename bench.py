@@ -63,6 +63,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-c2", action="store_true", help="skip the C2 batched-launch report")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the C3/C4 surrogate report")
+    ap.add_argument("--c3-pairs", type=float, default=5e5,
+                    help="training pairs of the C3 report (the full table is 2e6)")
+    ap.add_argument("--c3-steps", type=int, default=6000)
+    ap.add_argument("--c4-pairs", type=float, default=1e6)
     return ap.parse_args()
 
 
@@ -280,6 +285,115 @@ def bench_c2(pp, torch, local, reps=3):
                        "safety_cell_m": round(float(t.safety_cell), 2)}}
 
 
+def bench_surrogate(pp, torch, local, args):
+    """C3: MC tables (1e5 photons per pair, histogram mode) and Adam training
+    of the 8 -> 4x256 SiLU -> 1+64 network at batch 8192, lr 1e-3.
+    C4: one batch of 1e6 pairs answered by the fused inference kernel, 1% of
+    pairs audited by the MC at 1e7 photons (the judge), errors of the network
+    against it on the audited pairs with at least 400 MC hits."""
+    s = pp.surrogate
+    ctx = pp.Context(local)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    table_ph = 100_000
+    n3 = int(args.c3_pairs)
+    pairs = s.sample_pairs(n3, seed=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    c, h = s.generate_tables(pairs, table_ph, seed=1, ctx=ctx, device_out=True)
+    t_tab = time.perf_counter() - t0
+    x = torch.tensor(s.pair_features(pairs), device="cuda")
+    mlp = s.MLP(device=local, max_batch=8192, seed=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    log = s.train(mlp, x, c, h, steps=args.c3_steps, batch=8192, lr=1e-3,
+                  log_every=max(1, args.c3_steps // 20))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    # one training step timed alone with events (forward, backward, Adam)
+    bi = torch.randint(0, n3, (8192,), device="cuda")
+    bx, bc, bh = x[bi].contiguous(), c[bi].contiguous(), h[bi].contiguous()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cur = torch.cuda.current_stream().cuda_stream
+    e0.record()
+    for _ in range(20):
+        mlp.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), 8192, 1e-6, stream=cur)
+    e1.record()
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1) / 20
+    flops_row = 2 * sum(r * cc for r, cc in
+                        (mlp.layout(l)[2:] for l in range(mlp.n_layers + 1)))
+    # C4
+    n4 = int(args.c4_pairs)
+    ev = s.sample_pairs(n4, seed=4)
+    xb = torch.tensor(s.pair_features(ev), device="cuda")
+    eb = torch.empty(n4, device="cuda")
+    pb = torch.empty((n4, s.N_BINS), device="cuda")
+    for _ in range(3):
+        mlp.infer(xb.data_ptr(), n4, eb.data_ptr(), pb.data_ptr(), stream=cur, check_now=False)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(10):
+        mlp.infer(xb.data_ptr(), n4, eb.data_ptr(), pb.data_ptr(), stream=cur, check_now=False)
+    e1.record()
+    torch.cuda.synchronize()
+    mlp.infer(xb.data_ptr(), n4, eb.data_ptr(), pb.data_ptr())  # checks the error flag
+    infer_ms = e0.elapsed_time(e1) / 10
+    sur = s.Surrogate(mlp, table_photons=table_ph, ctx=ctx)
+    t0 = time.perf_counter()
+    r = sur.expectations(ev, photons=table_ph, seed=5)
+    t_batch = time.perf_counter() - t0
+    a = r.audit
+    mc_rate = a["mc_pairs"] / a["mc_seconds"] if a["mc_seconds"] > 0 else None
+    # the methods without the network, on the audited pairs the MC judged
+    aud = np.flatnonzero(r.from_mc)
+    judge = r.counts[aud] * (1e7 / table_ph)
+    ok = judge >= 400
+    gain = None
+    if ok.sum() >= 5:
+        sub = ev.subset(aud[ok])
+        lc, _ = s.generate_tables(sub, table_ph, seed=6, ctx=ctx)
+        rel_mc = np.abs(lc * (1e7 / table_ph) - judge[ok]) / judge[ok]
+        norm = s.fit_analytic_norm(sub, judge[ok], 1e7)
+        rel_an = np.abs(s.analytic_expectation(sub, 1e7, norm=norm) - judge[ok]) / judge[ok]
+        gain = {"equal_cost_mc_1e5_median_rel_error": float(np.median(rel_mc)),
+                "analytic_scaling_median_rel_error": float(np.median(rel_an)),
+                "analytic": "norm*N*r^2/(4d^2)*exp(-d/25 m), norm fitted to the judge"}
+    mlp.close()
+    ctx.close()
+    bf16_peak = peaks.get("bf16_tflops")
+    infer_tflops = flops_row * n4 / (infer_ms * 1e-3) / 1e12
+    return {
+        "c3_training": {
+            "workload": f"{n3} pairs (d log-uniform [5, 300] m, directions uniform), "
+                        f"{table_ph} photons per pair, cascades a=2.0 b=0.63 lrad=0.36 m, "
+                        "targets: count + 64-bin log10(t_res+21 ns) histogram",
+            "table_photons_per_s": n3 * table_ph / t_tab, "table_seconds": t_tab,
+            "train_steps": args.c3_steps, "batch": 8192, "lr": 1e-3,
+            "train_seconds": t_train, "train_step_ms": step_ms,
+            "train_tflops": 3 * flops_row * 8192 / (step_ms * 1e-3) / 1e12,
+            "loss_first": log[0][1], "loss_last": log[-1][1]},
+        "c4_inference": {
+            "workload": f"{n4} pairs from the training distributions; 1% audited by the MC "
+                        "at 1e7 photons per pair",
+            "nn_module_expectations_per_s": n4 / (infer_ms * 1e-3),
+            "infer_ms": infer_ms,
+            "roofline": {"bound": "tensor", "achieved": infer_tflops, "peak": bf16_peak,
+                         "unit": "TFLOP/s",
+                         "frac": infer_tflops / bf16_peak if bf16_peak else None,
+                         "note": f"{flops_row} FLOPs per pair; peak = measured cuBLAS bf16"},
+            "batch_module_expectations_per_s": n4 / t_batch, "batch_seconds": t_batch,
+            "mc_1e7_module_expectations_per_s": mc_rate,
+            "speedup_nn_only": (n4 / (infer_ms * 1e-3)) / mc_rate if mc_rate else None,
+            "speedup_with_audit": (n4 / t_batch) / mc_rate if mc_rate else None,
+            "audit": a, "without_network": gain},
+    }
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -392,6 +506,7 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_photons * world / e2e_s
     c2 = None if (world > 1 or args.no_c2 or args.config != "c1") else bench_c2(pp, torch, local)
+    sur = None if (world > 1 or args.no_surrogate) else bench_surrogate(pp, torch, local, args)
 
     if rank != 0:
         return 0
@@ -435,6 +550,7 @@ def run_ours(args):
         "clocks": clocks.summary(),
         "gpu_launches": args.steps,
         "c2_batched": c2,
+        "surrogate": sur,
         "wall_s_timed_region": wall,
     }
     print(json.dumps(line))

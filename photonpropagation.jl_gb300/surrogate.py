@@ -96,6 +96,23 @@ def geometric_time(p: Pairs, medium=None) -> np.ndarray:
     return (p.distance - MODULE_RADIUS) / float(medium.group_velocity(800.0))
 
 
+def cascade_records(pairs: Pairs, photons: int):
+    """The pp_source records of table_setup's emitters, filled column-wise
+    (the same bytes as converting each ExtendedCherenkovEmitter)."""
+    n = len(pairs)
+    rec = np.zeros(max(1, n), dtype=np.dtype(_lib.pp_source))
+    rec["kind"][:n] = _lib.PP_SRC_EXTENDED_CHERENKOV
+    rec["photons"][:n] = int(photons)
+    rec["position"][:n] = source_positions(pairs).astype(np.float32)
+    rec["direction"][:n] = pairs.emitter_dir.astype(np.float32)
+    rec["long_a"][:n] = CASCADE.a
+    rec["long_b"][:n] = CASCADE.b
+    rec["long_lrad"][:n] = CASCADE.lrad
+    arr = (_lib.pp_source * max(1, n)).from_buffer(rec)
+    arr._keep = rec
+    return arr
+
+
 def table_setup(pairs: Pairs, photons: int, seed: int, medium=None, spectrum=None):
     """One PhotonPropSetup holding every pair: the module at the origin and one
     ExtendedCherenkovEmitter per pair (source index = pair index)."""
@@ -130,14 +147,10 @@ def generate_tables(pairs: Pairs, photons: int, seed: int = 1, ctx=None, medium=
     hists = torch.empty((n, N_BINS), dtype=torch.float32, device="cuda")
     ctr = torch.zeros(64, dtype=torch.uint8, device="cuda")
     tgeo_all = torch.tensor(geometric_time(pairs, medium), dtype=torch.float32, device="cuda")
-    first = True
+    table_setup(pairs.subset(slice(0, 1)), photons, seed, medium, spectrum).upload(ctx)
     for lo in range(0, n, chunk):
         hi = min(n, lo + chunk)
-        setup = table_setup(pairs.subset(slice(lo, hi)), photons, seed + lo, medium, spectrum)
-        if first:
-            setup.upload(ctx)
-            first = False
-        ctx.set_sources(setup.source_records(), hi - lo, 1.0)
+        ctx.set_sources(cascade_records(pairs.subset(slice(lo, hi)), photons), hi - lo, 1.0)
         hist = torch.empty((hi - lo, N_BINS + 1), dtype=torch.float32, device="cuda")
         check(ctx._lib.pp_launch_histogram(ctx.ptr, seed + lo, n_steps,
                                            c_void_p(tgeo_all[lo:hi].data_ptr()),
@@ -378,19 +391,25 @@ class Surrogate:
 
     def expectations(self, p: Pairs, photons: float | None = None, seed: int = 0,
                      with_pdf: bool = True) -> Expectations:
+        import time
         photons = self.table_photons if photons is None else float(photons)
         n = len(p)
+        t0 = time.perf_counter()
         counts_d, pdf_d = self.infer(p, with_pdf)
         counts = counts_d.cpu().numpy().astype(np.float64) * (photons / self.table_photons)
         pdf = pdf_d.cpu().numpy() if with_pdf else None
+        t_nn = time.perf_counter() - t0
         rng = np.random.default_rng(seed)
         inside = in_training_range(p)
         audit = np.flatnonzero(inside & (rng.random(n) < self.audit_fraction))
         mc_idx = np.union1d(np.flatnonzero(~inside), audit)
         from_mc = np.zeros(n, bool)
-        stats = {"n_pairs": n, "n_outside": int((~inside).sum()), "n_audited": int(audit.size)}
+        stats = {"n_pairs": n, "n_outside": int((~inside).sum()), "n_audited": int(audit.size),
+                 "nn_seconds": t_nn, "mc_pairs": int(mc_idx.size), "mc_seconds": 0.0}
         if mc_idx.size:
+            t0 = time.perf_counter()
             mc_c, mc_h = self._mc(p.subset(mc_idx), seed)
+            stats["mc_seconds"] = time.perf_counter() - t0
             scale = photons / self.fallback_photons
             pos = np.searchsorted(mc_idx, audit)
             judged = mc_c[pos] >= self.min_audit_hits
@@ -418,7 +437,10 @@ class Surrogate:
         if failed and self.on_failure == "mc":
             rest = np.flatnonzero(~from_mc)
             if rest.size:
+                t0 = time.perf_counter()
                 mc_c, mc_h = self._mc(p.subset(rest), seed + 1)
+                stats["mc_seconds"] += time.perf_counter() - t0
+                stats["mc_pairs"] += int(rest.size)
                 counts[rest] = mc_c * (photons / self.fallback_photons)
                 if with_pdf:
                     pdf[rest] = self._normalise(mc_h)

@@ -42,6 +42,14 @@ def test_pair_features(pp):
     assert not np.any(s.in_training_range(out))
 
 
+def test_cascade_records_match_emitter_records(pp):
+    s = pp.surrogate
+    p = s.sample_pairs(50, seed=6)
+    fast = s.cascade_records(p, 123_456)
+    slow = s.table_setup(p, 123_456, seed=1).source_records()
+    assert bytes(fast) == bytes(slow)
+
+
 def oracle_histograms(orc, pp, pairs, photons, seed, n_bins):
     """Counts and log-residual-time histograms from the oracle's hit lists,
     binned with the kernel's FP32 arithmetic."""
