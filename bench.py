@@ -68,6 +68,8 @@ def parse_args():
                     help="training pairs of the C3 report (the full table is 2e6)")
     ap.add_argument("--c3-steps", type=int, default=6000)
     ap.add_argument("--c4-pairs", type=float, default=1e6)
+    ap.add_argument("--surrogate-only", action="store_true",
+                    help="print only the C3/C4 surrogate report (for profiling its kernels)")
     return ap.parse_args()
 
 
@@ -343,7 +345,8 @@ def bench_surrogate(pp, torch, local, args):
     torch.cuda.synchronize()
     mlp.infer(xb.data_ptr(), n4, eb.data_ptr(), pb.data_ptr())  # checks the error flag
     infer_ms = e0.elapsed_time(e1) / 10
-    sur = s.Surrogate(mlp, table_photons=table_ph, ctx=ctx)
+    # a failed audit is reported (audit.passed) rather than re-run through the MC
+    sur = s.Surrogate(mlp, table_photons=table_ph, ctx=ctx, on_failure="flag")
     t0 = time.perf_counter()
     r = sur.expectations(ev, photons=table_ph, seed=5)
     t_batch = time.perf_counter() - t0
@@ -561,6 +564,12 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.surrogate_only:
+        import torch
+        _, _, local = dist_env()
+        torch.cuda.set_device(local)
+        print(json.dumps({"surrogate": bench_surrogate(entry.load(), torch, local, args)}))
+        return 0
     return run_ours(args)
 
 

@@ -300,24 +300,48 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* _
   if (i < n) y[i] = __float2bfloat16(x[i]);
 }
 
-// Weights of layer l in the core-matrix layout the tensor core reads, so that
-// the fused kernel can copy a whole layer into shared memory with one TMA
-// bulk copy: element (r, c) of the rows x cols matrix at byte
-// core_offset(r, c / 8, cols) + (c % 8) * 2.
+// ---------------------------------------------------------------------------
+// Fused inference.
+//
+// Weights are packed once per parameter update into K-chunks of kChunkK
+// columns (the last chunk of a layer may be 16 wide), each chunk a contiguous
+// block in the tensor core's core-matrix layout: element (r, c) of layer l
+// (rows x cols) at
+//   wpack_off[l] + (c / kChunkK) * rows * kChunkK * 2
+//   + core_offset(r, (c % kChunkK) / 8, chunk width) + (c % 8) * 2,
+// so that one TMA bulk copy brings one chunk into a ring slot.
+constexpr int kChunkK = 32;
+constexpr int kRingSlots = 4;
+constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 32 BF16
+
+__host__ __device__ inline int chunk_width(int K, int j) {
+  return K - j * kChunkK < kChunkK ? K - j * kChunkK : kChunkK;
+}
+
 __global__ void repack_kernel(const bf16* __restrict__ w, int rows, int cols,
                               unsigned char* __restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (long long)rows * cols) return;
   const int r = (int)(i / cols), c = (int)(i % cols);
-  *reinterpret_cast<bf16*>(out + pptc::core_offset(r, c >> 3, cols) + (c & 7) * 2) = w[i];
+  const int j = c / kChunkK, cc = c % kChunkK;
+  const size_t off = (size_t)j * rows * kChunkK * 2 +
+                     pptc::core_offset(r, cc >> 3, chunk_width(cols, j)) + (cc & 7) * 2;
+  *reinterpret_cast<bf16*>(out + off) = w[i];
 }
 
 constexpr int kMaxLayers = 17;
+constexpr int kEpiWarps = 16;                        // epilogue warps (4 per TMEM lane quarter)
+constexpr int kEpiThreads = kEpiWarps * 32;
+constexpr int kInferThreads = 64 + kEpiThreads;      // producer warp, MMA warp, epilogue
 struct InferParams {
   const float* x;
   long long n;
   int n_in, in_pad, hidden, n_layers, out_pad, n_bins;
-  uint32_t tmem_cols;               // power of two >= 32 covering hidden and out_pad
+  int n_tiles;
+  uint32_t slot_cols;               // TMEM columns per accumulator (power of two >= 32)
+  uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) BF16)
+  uint32_t ring_off, bias_off;      // shared-memory byte offsets
+  int stage_pdf;                    // PDF rows staged through shared memory
   const unsigned char* wpack;
   long long wpack_off[kMaxLayers];  // bytes, multiples of 512
   const float* P;                   // FP32 parameters (biases)
@@ -327,163 +351,320 @@ struct InferParams {
   unsigned* err;
 };
 
-// The whole network for 128 rows in one CTA: the activations never leave
-// shared memory (core-matrix layout, the A operand of the next layer), each
-// layer's packed weights arrive by TMA bulk copies into a second buffer (the
-// B operand), the accumulator is 128 lanes x N columns of tensor memory.  The
-// head epilogue turns column 0 into the expected count exp(min(o, 30)) and
-// columns 1..n_bins into a softmax, staged through shared memory so that the
-// PDF rows are stored coalesced.
-__global__ void __launch_bounds__(128, 1) infer_kernel(const __grid_constant__ InferParams p) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bar_mma;
-  __shared__ __align__(8) uint64_t bar_tma;
-  __shared__ uint32_t tmem_slot;
-  const int act_k = p.hidden > p.in_pad ? p.hidden : p.in_pad;
-  unsigned char* sA = smem;
-  unsigned char* sW = smem + (size_t)128 * act_k * 2;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long row0 = (long long)blockIdx.x * 128;
-  const int r = warp * 32 + lane;  // this thread's row in the tile = its TMEM lane
-  const long long row = row0 + r;
-  if (warp == 0) pptc::tmem_alloc(&tmem_slot, p.tmem_cols);
-  if (threadIdx.x == 0) {
-    pptc::mbar_init(&bar_mma, 1);
-    pptc::mbar_init(&bar_tma, 1);
+// The sequence of jobs every role walks through in the same order: rounds of
+// two tiles (slot 0 and slot 1 of this CTA), each round all layers, the two
+// slots alternating per layer, so that the tensor core works on one slot
+// while the epilogue warps drain the other.
+struct JobIter {
+  int round = 0, layer = 0, slot = 0;
+  __device__ int tile(const InferParams& p) const {
+    return (round * (int)gridDim.x + (int)blockIdx.x) * 2 + slot;
   }
-  for (int kb = 0; kb < p.in_pad / 8; ++kb) {
+  __device__ bool valid(const InferParams& p) const { return tile(p) < p.n_tiles; }
+  // advance to the next valid job; false when the CTA's work is done
+  __device__ bool next(const InferParams& p) {
+    while (true) {
+      if (slot == 0) {
+        slot = 1;
+      } else {
+        slot = 0;
+        if (++layer > p.n_layers) {
+          layer = 0;
+          ++round;
+          if ((round * (int)gridDim.x + (int)blockIdx.x) * 2 >= p.n_tiles) return false;
+        }
+      }
+      if (valid(p)) return true;
+    }
+  }
+};
+
+__device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* act, int tile,
+                                           int t) {
+  const long long row0 = (long long)tile * 128;
+  for (int u = t; u < 128 * (p.in_pad / 8); u += kEpiThreads) {
+    const int rr = u & 127, kb = u >> 7;
+    const long long xr = row0 + rr;
     union {
-      uint4 u;
+      uint4 u4;
       bf16 h[8];
     } v;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int c = kb * 8 + j;
-      v.h[j] = __float2bfloat16(row < p.n && c < p.n_in ? p.x[row * p.n_in + c] : 0.0f);
+      v.h[j] = __float2bfloat16(xr < p.n && c < p.n_in ? p.x[xr * p.n_in + c] : 0.0f);
     }
-    *reinterpret_cast<uint4*>(sA + pptc::core_offset(r, kb, p.in_pad)) = v.u;
+    *reinterpret_cast<uint4*>(act + pptc::core_offset(rr, kb, p.in_pad)) = v.u4;
+  }
+}
+
+__device__ __forceinline__ void epi_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+}
+
+// Barrier over the epilogue warps that also ANDs a flag across them, so that
+// all of them take the same branch after a bounded wait.
+__device__ __forceinline__ bool epi_all(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(kEpiThreads)
+      : "memory");
+  return r != 0;
+}
+
+// Persistent, warp-specialised network evaluation, 256 rows (two tiles of
+// 128) in flight per CTA:
+//   warp 0      streams weight chunks into a kRingSlots-deep ring (TMA bulk
+//               copies, one mbarrier per slot and direction);
+//   warp 1      issues the tcgen05 MMAs of a job (one thread) once the slot's
+//               activations are ready, releasing each ring slot by commit;
+//   warps 2..17 the epilogue: bias + SiLU back into the slot's activations
+//               (in place: the MMAs that read them have completed), or the
+//               head (expected count exp(min(o, 30)) and softmax PDF), then
+//               the slot's next input tile.
+// Warp w reads TMEM lanes 32 (w % 4) .. + 31.  Every wait is bounded; a
+// timeout sets the error flag and the roles wind down (copies and MMAs in
+// flight are waited for, again bounded, before TMEM is released).
+__global__ void __launch_bounds__(kInferThreads, 1)
+    infer_kernel(const __grid_constant__ InferParams p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t w_full[kRingSlots], w_empty[kRingSlots];
+  __shared__ __align__(8) uint64_t acc_full[2], act_ready[2], mma_done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  unsigned char* ring = smem + p.ring_off;
+  float* sBias = reinterpret_cast<float*>(smem + p.bias_off);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) pptc::tmem_alloc(&tmem_slot, 2 * p.slot_cols);
+  if (threadIdx.x == 32) {
+    for (int i = 0; i < kRingSlots; ++i) {
+      pptc::mbar_init(&w_full[i], 1);
+      pptc::mbar_init(&w_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      pptc::mbar_init(&acc_full[i], 1);
+      pptc::mbar_init(&act_ready[i], kEpiThreads);
+    }
+    pptc::mbar_init(&mma_done, 1);
+    abort_flag = 0;
+  }
+  for (int l = 0; l <= p.n_layers; ++l) {
+    const int rows = l == p.n_layers ? p.out_pad : p.hidden;
+    for (int j = threadIdx.x; j < rows; j += kInferThreads)
+      sBias[l * p.hidden + j] = p.P[p.off_b[l] + j];
   }
   pptc::fence_before_sync();
   __syncthreads();
   pptc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
   bool ok = true;
-  int kin = p.in_pad;
-  for (int l = 0; l <= p.n_layers; ++l) {
-    const bool head = l == p.n_layers;
-    const int rows = head ? p.out_pad : p.hidden;
-    const uint32_t wbytes = (uint32_t)rows * (uint32_t)kin * 2u;
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-                       pptc::smem_u32(&bar_tma)),
-                   "r"(wbytes)
-                   : "memory");
-      for (uint32_t off = 0; off < wbytes; off += 32768) {
-        const uint32_t nb = wbytes - off < 32768 ? wbytes - off : 32768;
-        asm volatile(
-            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-            "[%3];" ::"r"(pptc::smem_u32(sW + off)),
-            "l"(p.wpack + p.wpack_off[l] + off), "r"(nb), "r"(pptc::smem_u32(&bar_tma))
-            : "memory");
+
+  if (warp == 0) {
+    // ---------------- weight producer
+    if (lane == 0) {
+      JobIter it;
+      bool more = it.valid(p);
+      uint32_t k = 0;  // chunks issued
+      while (more && ok) {
+        const int l = it.layer;
+        const int K = l == 0 ? p.in_pad : p.hidden;
+        const int rows = l == p.n_layers ? p.out_pad : p.hidden;
+        for (int j = 0; j * kChunkK < K; ++j, ++k) {
+          const uint32_t slot = k % kRingSlots, use = k / kRingSlots;
+          if (abort_flag || !pptc::mbar_wait(&w_empty[slot], (use & 1) ^ 1, kWaitNs)) {
+            ok = false;
+            break;
+          }
+          const uint32_t bytes = (uint32_t)rows * chunk_width(K, j) * 2u;
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                           pptc::smem_u32(&w_full[slot])),
+                       "r"(bytes)
+                       : "memory");
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+              "%2, [%3];" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
+              "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
+              "r"(pptc::smem_u32(&w_full[slot]))
+              : "memory");
+        }
+        more = it.next(p);
+      }
+      if (!ok) {
+        abort_flag = 1;
+        // let the copies still in flight land before shared memory is released
+        for (uint32_t q = k > kRingSlots ? k - kRingSlots : 0; q < k; ++q)
+          pptc::mbar_wait(&w_full[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
       }
     }
-    pptc::fence_async_smem();  // this thread's activation writes -> tensor-core reads
-    if (!__syncthreads_and(pptc::mbar_wait(&bar_tma, (uint32_t)(l & 1), kWaitNs))) {
-      // let the copies in flight land before the shared memory is released
-      pptc::mbar_wait(&bar_tma, (uint32_t)(l & 1), kWaitNs);
-      ok = false;
-      break;
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      JobIter it;
+      bool more = it.valid(p);
+      uint32_t k = 0;                   // chunks consumed
+      uint32_t jobs[2] = {0u, 0u};      // jobs issued per slot
+      while (more && ok) {
+        const int T = it.slot, l = it.layer;
+        const int K = l == 0 ? p.in_pad : p.hidden;
+        const int N = l == p.n_layers ? p.out_pad : p.hidden;
+        if (abort_flag || !pptc::mbar_wait(&act_ready[T], jobs[T] & 1, kWaitNs)) {
+          ok = false;
+          break;
+        }
+        pptc::fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)T * p.slot_cols;
+        const uint32_t a_base = pptc::smem_u32(smem + (size_t)T * p.act_bytes);
+        const uint32_t a_sbo = (uint32_t)(K / 8) * 128u;
+        const uint32_t idesc = pptc::idesc_bf16(128, N);
+        for (int j = 0; j * kChunkK < K; ++j, ++k) {
+          const uint32_t slot = k % kRingSlots, use = k / kRingSlots;
+          if (abort_flag || !pptc::mbar_wait(&w_full[slot], use & 1, kWaitNs)) {
+            ok = false;
+            break;
+          }
+          pptc::fence_after_sync();
+          const int w = chunk_width(K, j);
+          const uint32_t b_base = pptc::smem_u32(ring + slot * kSlotBytes);
+          const uint32_t b_sbo = (uint32_t)(w / 8) * 128u;
+          for (int s = 0; s < w / 16; ++s) {
+            const uint64_t ad = pptc::smem_desc(a_base + (uint32_t)(j * (kChunkK / 16) + s) * 256u,
+                                                128, a_sbo);
+            const uint64_t bd = pptc::smem_desc(b_base + (uint32_t)s * 256u, 128, b_sbo);
+            pptc::mma_bf16(d, ad, bd, idesc, j > 0 || s > 0);
+          }
+          pptc::mma_commit(&w_empty[slot]);  // the slot is free once these MMAs complete
+        }
+        if (!ok) break;
+        pptc::mma_commit(&acc_full[T]);
+        jobs[T]++;
+        more = it.next(p);
+      }
+      // everything issued has completed before TMEM and shared memory go away
+      pptc::mma_commit(&mma_done);
+      if (!pptc::mbar_wait(&mma_done, 0, kWaitNs)) ok = false;
+      if (!ok) abort_flag = 1;
     }
-    if (threadIdx.x == 0) {
+    __syncwarp();
+  } else {
+    // ---------------- epilogue
+    const int t = threadIdx.x - 64;
+    const int ew = warp - 2;
+    const int quad = warp & 3;  // TMEM lane quarter this warp may access
+    const int cgrp = ew >> 2;   // column group 0..3
+    const int r = quad * 32 + lane;
+    // first tiles of both slots
+    for (int T = 0; T < 2; ++T) {
+      const int tile = (int)blockIdx.x * 2 + T;
+      if (tile < p.n_tiles) pack_input(p, smem + (size_t)T * p.act_bytes, tile, t);
+      pptc::fence_async_smem();
+      pptc::mbar_arrive(&act_ready[T]);
+    }
+    JobIter it;
+    bool more = it.valid(p);
+    uint32_t jobs[2] = {0u, 0u};
+    while (more) {
+      const int T = it.slot, l = it.layer;
+      unsigned char* act = smem + (size_t)T * p.act_bytes;
+      if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, kWaitNs))) {
+        ok = false;
+        break;
+      }
+      jobs[T]++;
       pptc::fence_after_sync();
-      const uint32_t sbo = (uint32_t)(kin / 8) * 128u;
-      const uint32_t idesc = pptc::idesc_bf16(128, rows);
-      for (int s = 0; s < kin / 16; ++s) {
-        const uint64_t ad = pptc::smem_desc(pptc::smem_u32(sA) + s * 256, 128, sbo);
-        const uint64_t bd = pptc::smem_desc(pptc::smem_u32(sW) + s * 256, 128, sbo);
-        pptc::mma_bf16(tmem, ad, bd, idesc, s > 0);
-      }
-      pptc::mma_commit(&bar_mma);
-    }
-    if (!__syncthreads_and(pptc::mbar_wait(&bar_mma, (uint32_t)(l & 1), kWaitNs))) {
-      pptc::mbar_wait(&bar_mma, (uint32_t)(l & 1), kWaitNs);
-      ok = false;
-      break;
-    }
-    pptc::fence_after_sync();
-    const float* bias = p.P + p.off_b[l];
-    if (!head) {
-      for (int c0 = 0; c0 < p.hidden; c0 += 32) {
-        float v[32];
-        pptc::tmem_ld32(trow + (uint32_t)c0, v);
+      const uint32_t trow = tmem + (uint32_t)T * p.slot_cols + ((uint32_t)(quad * 32) << 16);
+      const float* bias = sBias + l * p.hidden;
+      if (l < p.n_layers) {
+        for (int c0 = cgrp * 32; c0 < p.hidden; c0 += 128) {
+          float v[32];
+          pptc::tmem_ld32(trow + (uint32_t)c0, v);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          if (c0 + q * 8 >= p.hidden) break;
-          union {
-            uint4 u;
-            bf16 h[8];
-          } o;
+          for (int q = 0; q < 4; ++q) {
+            if (c0 + q * 8 >= p.hidden) break;
+            union {
+              uint4 u4;
+              bf16 h[8];
+            } o;
 #pragma unroll
-          for (int j = 0; j < 8; ++j)
-            o.h[j] = __float2bfloat16(pptc::silu(v[q * 8 + j] + bias[c0 + q * 8 + j]));
-          *reinterpret_cast<uint4*>(sA + pptc::core_offset(r, (c0 >> 3) + q, p.hidden)) = o.u;
+            for (int j = 0; j < 8; ++j)
+              o.h[j] = __float2bfloat16(pptc::silu(v[q * 8 + j] + bias[c0 + q * 8 + j]));
+            *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (c0 >> 3) + q, p.hidden)) = o.u4;
+          }
         }
+      } else {
+        // head: warps of column group 0 own one row each
+        const long long row0 = (long long)it.tile(p) * 128;
+        const long long row = row0 + r;
+        const int ld = p.n_bins + 1;  // odd stride: the 32 rows of a warp hit 32 banks
+        float* stage = reinterpret_cast<float*>(act);
+        if (cgrp == 0) {
+          float o0 = 0.0f, mx = -INFINITY;
+          for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
+            float v[32];
+            pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int c = c0 + i;
+              if (c == 0) o0 = v[i] + bias[0];
+              else if (c <= p.n_bins) mx = fmaxf(mx, v[i] + bias[c]);
+            }
+          }
+          float se = 0.0f;
+          for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
+            float v[32];
+            pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int c = c0 + i;
+              if (c >= 1 && c <= p.n_bins) se += __expf(v[i] + bias[c] - mx);
+            }
+          }
+          if (row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
+          if (p.pdf) {
+            const float inv = 1.0f / se;
+            for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
+              float v[32];
+              pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll
+              for (int i = 0; i < 32; ++i) {
+                const int c = c0 + i;
+                if (c >= 1 && c <= p.n_bins) {
+                  const float pr = __expf(v[i] + bias[c] - mx) * inv;
+                  if (p.stage_pdf) stage[r * ld + c - 1] = pr;
+                  else if (row < p.n) p.pdf[row * p.n_bins + c - 1] = pr;
+                }
+              }
+            }
+          }
+        }
+        if (p.pdf && p.stage_pdf) {
+          epi_sync();
+          const long long left = p.n - row0;
+          const int nrows = left < 128 ? (int)left : 128;
+          float* dst = p.pdf + row0 * p.n_bins;
+          for (int i = t; i < nrows * p.n_bins; i += kEpiThreads)
+            dst[i] = stage[(i / p.n_bins) * ld + i % p.n_bins];
+        }
+        epi_sync();  // the slot's buffer is read out before the next input lands
+        const int next = it.tile(p) + 2 * (int)gridDim.x;
+        if (next < p.n_tiles) pack_input(p, act, next, t);
       }
-      kin = p.hidden;
+      pptc::fence_async_smem();  // activation writes -> the next MMAs of this slot
       pptc::fence_before_sync();
-      __syncthreads();
-      continue;
+      pptc::mbar_arrive(&act_ready[T]);
+      more = it.next(p);
     }
-    // head: pass 1 log count and softmax maximum, pass 2 the normaliser,
-    // pass 3 the probabilities into shared memory (all operands are consumed)
-    float o0 = 0.0f, mx = -INFINITY;
-    for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
-      float v[32];
-      pptc::tmem_ld32(trow + (uint32_t)c0, v);
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int c = c0 + i;
-        if (c == 0) o0 = v[i] + bias[0];
-        else if (c <= p.n_bins) mx = fmaxf(mx, v[i] + bias[c]);
-      }
-    }
-    float se = 0.0f;
-    for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
-      float v[32];
-      pptc::tmem_ld32(trow + (uint32_t)c0, v);
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int c = c0 + i;
-        if (c >= 1 && c <= p.n_bins) se += __expf(v[i] + bias[c] - mx);
-      }
-    }
-    if (row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
-    if (p.pdf) {
-      const float inv = 1.0f / se;
-      const int ld = p.n_bins + 1;  // odd stride: the 32 rows of a warp hit 32 banks
-      float* stage = reinterpret_cast<float*>(smem);
-      for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
-        float v[32];
-        pptc::tmem_ld32(trow + (uint32_t)c0, v);
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int c = c0 + i;
-          if (c >= 1 && c <= p.n_bins) stage[r * ld + c - 1] = __expf(v[i] + bias[c] - mx) * inv;
-        }
-      }
-      __syncthreads();
-      const long long left = p.n - row0;
-      const int nrows = left < 128 ? (int)left : 128;
-      float* dst = p.pdf + row0 * p.n_bins;
-      for (int i = threadIdx.x; i < nrows * p.n_bins; i += 128)
-        dst[i] = stage[(i / p.n_bins) * ld + i % p.n_bins];
-    }
+    if (!ok) abort_flag = 1;
   }
   pptc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) pptc::tmem_dealloc(tmem, p.tmem_cols);
-  if (!ok && threadIdx.x == 0) atomicOr(p.err, 1u);
+  if (warp == 0) pptc::tmem_dealloc(tmem, 2 * p.slot_cols);
+  if (threadIdx.x == 0 && (abort_flag || !ok)) atomicOr(p.err, 1u);
 }
 
 int fail(int code, const std::string& m) { return pp::report_error(code, m); }
@@ -539,6 +720,7 @@ struct pp_mlp {
   unsigned char* wpack = nullptr;       // BF16 weights in core-matrix layout
   std::vector<long long> wpack_off;     // bytes per layer
   bool pack_dirty = true;
+  int num_sms = 0;
   long long step = 0;
   float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f, time_weight = 1.0f;
 };
@@ -659,11 +841,21 @@ int mlp_repack(pp_mlp* m, cudaStream_t s) {
   return PP_OK;
 }
 
-size_t infer_smem_bytes(const pp_mlp* m) {
-  size_t w = 0;
-  for (int l = 0; l <= m->n_layers; ++l) w = std::max(w, (size_t)m->rows[l] * m->cols[l] * 2);
+// Shared memory of infer_kernel: the activations of two tiles (128 rows x
+// max(in_pad, hidden) BF16 each), the weight ring, then the biases.  The
+// head stages a tile's PDF rows (128 x (n_bins + 1) floats) in that tile's
+// activation buffer when they fit.
+struct InferSmem {
+  uint32_t act, ring_off, bias_off, total;
+  bool stage_pdf;
+};
+InferSmem infer_smem(const pp_mlp* m) {
   const size_t act = (size_t)128 * std::max(m->hidden, m->in_pad) * 2;
-  return std::max(act + w, (size_t)128 * (m->n_bins + 1) * 4);
+  const size_t ring_off = 2 * act;
+  const size_t bias_off = ring_off + (size_t)kRingSlots * kSlotBytes;
+  const size_t bias = sizeof(float) * ((size_t)m->n_layers * m->hidden + m->out_pad);
+  return {(uint32_t)act, (uint32_t)ring_off, (uint32_t)bias_off, (uint32_t)(bias_off + bias),
+          (size_t)128 * (m->n_bins + 1) * 4 <= act};
 }
 
 int check_err(pp_mlp* m, cudaStream_t s) {
@@ -912,29 +1104,39 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
   if (!m || !d_x || !d_expect || n < 0) return fail(PP_ERR_INVALID, "bad arguments");
   if (m->n_layers + 1 > kMaxLayers) return fail(PP_ERR_INVALID, "too many layers");
   if (n == 0) return PP_OK;
-  if ((n + 127) / 128 > 0x7FFFFFFFLL) return fail(PP_ERR_INVALID, "n too large");
+  if ((n + 127) / 128 > 0x3FFFFFFFLL) return fail(PP_ERR_INVALID, "n too large");
   cudaSetDevice(m->device);
   cudaStream_t s = (cudaStream_t)stream;
   if (m->pack_dirty) {
     int rc = mlp_repack(m, s);
     if (rc != PP_OK) return rc;
   }
-  const size_t smem = infer_smem_bytes(m);
+  const InferSmem sm = infer_smem(m);
+  const size_t smem = sm.total;
   cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "infer smem");
   InferParams p{};
   p.x = d_x; p.n = n; p.n_in = m->n_in; p.in_pad = m->in_pad; p.hidden = m->hidden;
   p.n_layers = m->n_layers; p.out_pad = m->out_pad; p.n_bins = m->n_bins;
-  p.tmem_cols = 32;
-  while (p.tmem_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.tmem_cols *= 2;
+  const long long tiles = (n + 127) / 128;
+  p.n_tiles = (int)tiles;
+  p.slot_cols = 32;
+  while (p.slot_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.slot_cols *= 2;
+  p.act_bytes = sm.act; p.ring_off = sm.ring_off; p.bias_off = sm.bias_off;
+  p.stage_pdf = sm.stage_pdf ? 1 : 0;
   p.wpack = m->wpack; p.P = m->P;
   for (int l = 0; l <= m->n_layers; ++l) {
     p.wpack_off[l] = m->wpack_off[l];
     p.off_b[l] = m->off_b[l];
   }
   p.expect = d_expect; p.pdf = d_pdf; p.err = m->err;
-  infer_kernel<<<(unsigned)((n + 127) / 128), 128, smem, s>>>(p);
+  if (m->num_sms == 0) {
+    e = cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device);
+    if (e != cudaSuccess) return cuda_fail(e, "SM count");
+  }
+  const long long grid = std::min<long long>(m->num_sms, (tiles + 1) / 2);
+  infer_kernel<<<(unsigned)grid, kInferThreads, smem, s>>>(p);
   e = cudaGetLastError();
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "infer kernel");
 }

@@ -155,8 +155,9 @@ def test_fused_inference_matches_oracle(pp, gpu_ctx, n, hidden, layers, n_bins):
     W, b = mlp.unpack(mlp.params())
     lam, p_ref = mlp_oracle.MLPOracle(W, b, 8, n_bins).predict(x)
     got_l, got_p = expect.cpu().numpy(), pdf.cpu().numpy()
-    # BF16 activations: one rounding flip moves an output by ~1e-3
-    np.testing.assert_allclose(got_l, lam, rtol=5e-3)
+    # BF16 activations (one rounding flip moves an output by ~1e-3) and the
+    # tanh.approx sigmoid (~2^-11): the log-count output agrees within 1e-2
+    np.testing.assert_allclose(np.log(got_l), np.log(lam), atol=1e-2)
     np.testing.assert_allclose(got_p.sum(axis=1), 1.0, rtol=1e-5)
     np.testing.assert_allclose(got_p, p_ref, rtol=1e-2, atol=1e-5)
     # the expected counts alone (no PDF output)
@@ -181,5 +182,5 @@ def test_fused_inference_follows_training(pp, gpu_ctx):
     assert not torch.equal(e0, e1)
     W, b = mlp.unpack(mlp.params())
     lam, _ = mlp_oracle.MLPOracle(W, b, 8, 64).predict(x)
-    np.testing.assert_allclose(e1.cpu().numpy(), lam, rtol=5e-3)
+    np.testing.assert_allclose(np.log(e1.cpu().numpy()), np.log(lam), atol=1e-2)
     mlp.close()
