@@ -311,7 +311,7 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* _
 //   + core_offset(r, (c % kChunkK) / 8, chunk width) + (c % 8) * 2,
 // so that one TMA bulk copy brings one chunk into a ring slot.
 constexpr int kChunkK = 32;
-constexpr int kRingSlots = 4;
+constexpr int kRingSlots = 5;
 constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 32 BF16
 
 __host__ __device__ inline int chunk_width(int K, int j) {
@@ -379,22 +379,33 @@ struct JobIter {
   }
 };
 
+// Input unit u of a tile: row u % 128, features 8 (u / 128) .. + 7 (zero
+// beyond n_in and past the last row).
+__device__ __forceinline__ void load_unit(const InferParams& p, int tile, int u, float* xin) {
+  const int rr = u & 127, kb = u >> 7;
+  const long long xr = (long long)tile * 128 + rr;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int c = kb * 8 + j;
+    xin[j] = xr < p.n && c < p.n_in ? p.x[xr * p.n_in + c] : 0.0f;
+  }
+}
+__device__ __forceinline__ void store_unit(const InferParams& p, unsigned char* act, int u,
+                                           const float* xin) {
+  union {
+    uint4 u4;
+    __nv_bfloat162 h2[4];
+  } v;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) v.h2[j] = __floats2bfloat162_rn(xin[2 * j], xin[2 * j + 1]);
+  *reinterpret_cast<uint4*>(act + pptc::core_offset(u & 127, u >> 7, p.in_pad)) = v.u4;
+}
 __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* act, int tile,
                                            int t) {
-  const long long row0 = (long long)tile * 128;
-  for (int u = t; u < 128 * (p.in_pad / 8); u += kEpiThreads) {
-    const int rr = u & 127, kb = u >> 7;
-    const long long xr = row0 + rr;
-    union {
-      uint4 u4;
-      bf16 h[8];
-    } v;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int c = kb * 8 + j;
-      v.h[j] = __float2bfloat16(xr < p.n && c < p.n_in ? p.x[xr * p.n_in + c] : 0.0f);
-    }
-    *reinterpret_cast<uint4*>(act + pptc::core_offset(rr, kb, p.in_pad)) = v.u4;
+  for (int u = t; u < 16 * p.in_pad; u += kEpiThreads) {
+    float xin[8];
+    load_unit(p, tile, u, xin);
+    store_unit(p, act, u, xin);
   }
 }
 
@@ -437,6 +448,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   __shared__ __align__(8) uint64_t acc_full[2], act_ready[2], mma_done;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
+  __shared__ float s_max[4][128], s_sum[4][128];  // head: per column group and row
   unsigned char* ring = smem + p.ring_off;
   float* sBias = reinterpret_cast<float*>(smem + p.bias_off);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -580,79 +592,127 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       const uint32_t trow = tmem + (uint32_t)T * p.slot_cols + ((uint32_t)(quad * 32) << 16);
       const float* bias = sBias + l * p.hidden;
       if (l < p.n_layers) {
-        for (int c0 = cgrp * 32; c0 < p.hidden; c0 += 128) {
-          float v[32];
-          pptc::tmem_ld32(trow + (uint32_t)c0, v);
+        // two 32-column slices per load-wait (columns c0 and c0 + 128)
+        for (int c0 = cgrp * 32; c0 < p.hidden; c0 += 256) {
+          uint32_t v[2][32];
+          const bool two = c0 + 128 < p.hidden;
+          pptc::tmem_ld32_nowait(trow + (uint32_t)c0, v[0]);
+          if (two) pptc::tmem_ld32_nowait(trow + (uint32_t)(c0 + 128), v[1]);
+          pptc::tmem_wait();
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (c0 + q * 8 >= p.hidden) break;
-            union {
-              uint4 u4;
-              bf16 h[8];
-            } o;
+          for (int h = 0; h < 2; ++h) {
+            if (h == 1 && !two) break;
+            const int cb = c0 + h * 128;
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-              o.h[j] = __float2bfloat16(pptc::silu(v[q * 8 + j] + bias[c0 + q * 8 + j]));
-            *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (c0 >> 3) + q, p.hidden)) = o.u4;
+            for (int q = 0; q < 4; ++q) {
+              if (cb + q * 8 >= p.hidden) break;
+              const float4 b0 = *reinterpret_cast<const float4*>(bias + cb + q * 8);
+              const float4 b1 = *reinterpret_cast<const float4*>(bias + cb + q * 8 + 4);
+              const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+              union {
+                uint4 u4;
+                __nv_bfloat162 h2[4];
+              } o;
+#pragma unroll
+              for (int j = 0; j < 4; ++j)
+                o.h2[j] = __floats2bfloat162_rn(
+                    pptc::silu(__uint_as_float(v[h][q * 8 + 2 * j]) + bb[2 * j]),
+                    pptc::silu(__uint_as_float(v[h][q * 8 + 2 * j + 1]) + bb[2 * j + 1]));
+              *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, p.hidden)) =
+                  o.u4;
+            }
           }
         }
       } else {
-        // head: warps of column group 0 own one row each
-        const long long row0 = (long long)it.tile(p) * 128;
+        // head: every epilogue warp takes the 32-column slices cgrp and
+        // cgrp + 4 of its 32 rows; row maximum and normaliser are combined
+        // across the four column groups in shared memory
+        const int tile = it.tile(p);
+        const long long row0 = (long long)tile * 128;
         const long long row = row0 + r;
         const int ld = p.n_bins + 1;  // odd stride: the 32 rows of a warp hit 32 banks
         float* stage = reinterpret_cast<float*>(act);
-        if (cgrp == 0) {
-          float o0 = 0.0f, mx = -INFINITY;
-          for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
-            float v[32];
-            pptc::tmem_ld32(trow + (uint32_t)c0, v);
+        // the slot's next input, loaded now so that its latency overlaps the head
+        const int next = tile + 2 * (int)gridDim.x;
+        const int units = 16 * p.in_pad;  // 128 rows x in_pad / 8 chunks of 8
+        const bool prefetch = units <= kEpiThreads;
+        float xin[8];
+        if (prefetch && t < units && next < p.n_tiles) load_unit(p, next, t, xin);
+        // pass 1: the log count and this warp's part of the row maximum
+        float o0 = 0.0f, mx = -INFINITY;
+#pragma unroll 1
+        for (int sl = cgrp; sl * 32 < p.out_pad; sl += 4) {
+          uint32_t v[32];
+          pptc::tmem_ld32_nowait(trow + (uint32_t)(sl * 32), v);
+          pptc::tmem_wait();
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
-              const int c = c0 + i;
-              if (c == 0) o0 = v[i] + bias[0];
-              else if (c <= p.n_bins) mx = fmaxf(mx, v[i] + bias[c]);
-            }
+          for (int i = 0; i < 32; ++i) {
+            const int c = sl * 32 + i;
+            if (c == 0) o0 = __uint_as_float(v[i]) + bias[0];
+            else if (c <= p.n_bins) mx = fmaxf(mx, __uint_as_float(v[i]) + bias[c]);
           }
+        }
+        if (cgrp == 0 && row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
+        if (p.pdf) {
+          s_max[cgrp][r] = mx;
+          epi_sync();
+          mx = fmaxf(fmaxf(s_max[0][r], s_max[1][r]), fmaxf(s_max[2][r], s_max[3][r]));
+          // pass 2: exponentials (into the staging rows, normalised on the way
+          // out) and this warp's part of the normaliser
           float se = 0.0f;
-          for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
-            float v[32];
-            pptc::tmem_ld32(trow + (uint32_t)c0, v);
+#pragma unroll 1
+          for (int sl = cgrp; sl * 32 < p.out_pad; sl += 4) {
+            uint32_t v[32];
+            pptc::tmem_ld32_nowait(trow + (uint32_t)(sl * 32), v);
+            pptc::tmem_wait();
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
-              const int c = c0 + i;
-              if (c >= 1 && c <= p.n_bins) se += __expf(v[i] + bias[c] - mx);
+              const int c = sl * 32 + i;
+              if (c >= 1 && c <= p.n_bins) {
+                const float e = __expf(__uint_as_float(v[i]) + bias[c] - mx);
+                se += e;
+                if (p.stage_pdf) stage[r * ld + c - 1] = e;
+              }
             }
           }
-          if (row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
-          if (p.pdf) {
-            const float inv = 1.0f / se;
-            for (int c0 = 0; c0 < p.out_pad; c0 += 32) {
-              float v[32];
-              pptc::tmem_ld32(trow + (uint32_t)c0, v);
+          s_sum[cgrp][r] = se;
+          epi_sync();
+          if (p.stage_pdf) {
+            const long long left = p.n - row0;
+            const int nrows = left < 128 ? (int)left : 128;
+            float* dst = p.pdf + row0 * p.n_bins;
+            for (int rr = ew; rr < nrows; rr += kEpiWarps) {
+              const float inv =
+                  1.0f / (s_sum[0][rr] + s_sum[1][rr] + s_sum[2][rr] + s_sum[3][rr]);
+              for (int c = lane; c < p.n_bins; c += 32)
+                dst[rr * p.n_bins + c] = stage[rr * ld + c] * inv;
+            }
+          } else {
+            // pass 3 (PDF rows too wide to stage): normalised values straight out
+            const float inv = 1.0f / (s_sum[0][r] + s_sum[1][r] + s_sum[2][r] + s_sum[3][r]);
+#pragma unroll 1
+            for (int sl = cgrp; sl * 32 < p.out_pad; sl += 4) {
+              uint32_t v[32];
+              pptc::tmem_ld32_nowait(trow + (uint32_t)(sl * 32), v);
+              pptc::tmem_wait();
 #pragma unroll
               for (int i = 0; i < 32; ++i) {
-                const int c = c0 + i;
-                if (c >= 1 && c <= p.n_bins) {
-                  const float pr = __expf(v[i] + bias[c] - mx) * inv;
-                  if (p.stage_pdf) stage[r * ld + c - 1] = pr;
-                  else if (row < p.n) p.pdf[row * p.n_bins + c - 1] = pr;
-                }
+                const int c = sl * 32 + i;
+                if (c >= 1 && c <= p.n_bins && row < p.n)
+                  p.pdf[row * p.n_bins + c - 1] =
+                      __expf(__uint_as_float(v[i]) + bias[c] - mx) * inv;
               }
             }
           }
         }
-        if (p.pdf && p.stage_pdf) {
-          epi_sync();
-          const long long left = p.n - row0;
-          const int nrows = left < 128 ? (int)left : 128;
-          float* dst = p.pdf + row0 * p.n_bins;
-          for (int i = t; i < nrows * p.n_bins; i += kEpiThreads)
-            dst[i] = stage[(i / p.n_bins) * ld + i % p.n_bins];
-        }
         epi_sync();  // the slot's buffer is read out before the next input lands
-        const int next = it.tile(p) + 2 * (int)gridDim.x;
-        if (next < p.n_tiles) pack_input(p, act, next, t);
+        if (next < p.n_tiles) {
+          if (prefetch) {
+            if (t < units) store_unit(p, act, t, xin);
+          } else {
+            pack_input(p, act, next, t);
+          }
+        }
       }
       pptc::fence_async_smem();  // activation writes -> the next MMAs of this slot
       pptc::fence_before_sync();
