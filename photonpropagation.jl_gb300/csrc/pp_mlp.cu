@@ -310,9 +310,10 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* _
 //   wpack_off[l] + (c / kChunkK) * rows * kChunkK * 2
 //   + core_offset(r, (c % kChunkK) / 8, chunk width) + (c % 8) * 2,
 // so that one TMA bulk copy brings one chunk into a ring slot.
-constexpr int kChunkK = 32;
-constexpr int kRingSlots = 5;
-constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 32 BF16
+constexpr int kChunkK = 64;
+constexpr int kRingSlots = 3;
+constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 64 BF16
+constexpr uint32_t kRedBytes = 2u * 4u * 128u * 4u;   // head: row max and sum per column group
 
 __host__ __device__ inline int chunk_width(int K, int j) {
   return K - j * kChunkK < kChunkK ? K - j * kChunkK : kChunkK;
@@ -333,14 +334,15 @@ constexpr int kMaxLayers = 17;
 constexpr int kEpiWarps = 16;                        // epilogue warps (4 per TMEM lane quarter)
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kInferThreads = 64 + kEpiThreads;      // producer warp, MMA warp, epilogue
+constexpr int kCluster = 2;  // CTAs sharing every weight chunk by TMA multicast
 struct InferParams {
   const float* x;
   long long n;
   int n_in, in_pad, hidden, n_layers, out_pad, n_bins;
-  int n_tiles;
+  int n_tiles, n_rounds;
   uint32_t slot_cols;               // TMEM columns per accumulator (power of two >= 32)
   uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) BF16)
-  uint32_t ring_off, bias_off;      // shared-memory byte offsets
+  uint32_t ring_off;                // shared-memory byte offset of the weight ring
   int stage_pdf;                    // PDF rows staged through shared memory
   const unsigned char* wpack;
   long long wpack_off[kMaxLayers];  // bytes, multiples of 512
@@ -354,30 +356,36 @@ struct InferParams {
 // The sequence of jobs every role walks through in the same order: rounds of
 // two tiles (slot 0 and slot 1 of this CTA), each round all layers, the two
 // slots alternating per layer, so that the tensor core works on one slot
-// while the epilogue warps drain the other.
+// while the epilogue warps drain the other.  Every CTA runs the same number
+// of rounds (the CTAs of a cluster consume one shared weight stream); tiles
+// past the last row are evaluated on zero rows and not stored.
 struct JobIter {
   int round = 0, layer = 0, slot = 0;
-  __device__ int tile(const InferParams& p) const {
-    return (round * (int)gridDim.x + (int)blockIdx.x) * 2 + slot;
-  }
-  __device__ bool valid(const InferParams& p) const { return tile(p) < p.n_tiles; }
-  // advance to the next valid job; false when the CTA's work is done
+  __device__ int tile() const { return (round * (int)gridDim.x + (int)blockIdx.x) * 2 + slot; }
+  // advance to the next job; false when the CTA's work is done
   __device__ bool next(const InferParams& p) {
-    while (true) {
-      if (slot == 0) {
-        slot = 1;
-      } else {
-        slot = 0;
-        if (++layer > p.n_layers) {
-          layer = 0;
-          ++round;
-          if ((round * (int)gridDim.x + (int)blockIdx.x) * 2 >= p.n_tiles) return false;
-        }
-      }
-      if (valid(p)) return true;
+    if (slot == 0) {
+      slot = 1;
+      return true;
     }
+    slot = 0;
+    if (++layer > p.n_layers) {
+      layer = 0;
+      if (++round >= p.n_rounds) return false;
+    }
+    return true;
   }
 };
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
 
 // Input unit u of a tile: row u % 128, features 8 (u / 128) .. + 7 (zero
 // beyond n_in and past the last row).
@@ -448,15 +456,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   __shared__ __align__(8) uint64_t acc_full[2], act_ready[2], mma_done;
   __shared__ uint32_t tmem_slot;
   __shared__ volatile int abort_flag;
-  __shared__ float s_max[4][128], s_sum[4][128];  // head: per column group and row
   unsigned char* ring = smem + p.ring_off;
-  float* sBias = reinterpret_cast<float*>(smem + p.bias_off);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) pptc::tmem_alloc(&tmem_slot, 2 * p.slot_cols);
   if (threadIdx.x == 32) {
     for (int i = 0; i < kRingSlots; ++i) {
       pptc::mbar_init(&w_full[i], 1);
-      pptc::mbar_init(&w_empty[i], 1);
+      pptc::mbar_init(&w_empty[i], kCluster);  // released by the MMAs of every CTA
     }
     for (int i = 0; i < 2; ++i) {
       pptc::mbar_init(&acc_full[i], 1);
@@ -465,13 +471,9 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     pptc::mbar_init(&mma_done, 1);
     abort_flag = 0;
   }
-  for (int l = 0; l <= p.n_layers; ++l) {
-    const int rows = l == p.n_layers ? p.out_pad : p.hidden;
-    for (int j = threadIdx.x; j < rows; j += kInferThreads)
-      sBias[l * p.hidden + j] = p.P[p.off_b[l] + j];
-  }
   pptc::fence_before_sync();
   __syncthreads();
+  cluster_sync();  // the peer's barriers are initialised before any copy or commit targets them
   pptc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   bool ok = true;
@@ -479,9 +481,10 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   if (warp == 0) {
     // ---------------- weight producer
     if (lane == 0) {
+      const uint32_t rank = cluster_rank();
       JobIter it;
-      bool more = it.valid(p);
-      uint32_t k = 0;  // chunks issued
+      bool more = true;
+      uint32_t k = 0;  // chunks of the shared stream seen
       while (more && ok) {
         const int l = it.layer;
         const int K = l == 0 ? p.in_pad : p.hidden;
@@ -492,25 +495,30 @@ __global__ void __launch_bounds__(kInferThreads, 1)
             ok = false;
             break;
           }
+          // every CTA expects each chunk; one CTA of the cluster fetches it
+          // for all (chunk k from CTA rank k % kCluster)
           const uint32_t bytes = (uint32_t)rows * chunk_width(K, j) * 2u;
           asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
                            pptc::smem_u32(&w_full[slot])),
                        "r"(bytes)
                        : "memory");
-          asm volatile(
-              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
-              "%2, [%3];" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
-              "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
-              "r"(pptc::smem_u32(&w_full[slot]))
-              : "memory");
+          if (k % kCluster == rank) {
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::"
+                "cluster [%0], [%1], %2, [%3], %4;" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
+                "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
+                "r"(pptc::smem_u32(&w_full[slot])), "h"((uint16_t)((1u << kCluster) - 1u))
+                : "memory");
+          }
         }
         more = it.next(p);
       }
-      if (!ok) {
-        abort_flag = 1;
-        // let the copies still in flight land before shared memory is released
-        for (uint32_t q = k > kRingSlots ? k - kRingSlots : 0; q < k; ++q)
-          pptc::mbar_wait(&w_full[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
+      if (!ok) abort_flag = 1;
+      // every slot is released by all CTAs (their commits have landed here)
+      // and every copy has landed before shared memory is given up
+      for (uint32_t q = k > kRingSlots ? k - kRingSlots : 0; q < k; ++q) {
+        pptc::mbar_wait(&w_full[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
+        pptc::mbar_wait(&w_empty[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
       }
     }
     __syncwarp();
@@ -518,7 +526,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     // ---------------- MMA issuer
     if (lane == 0) {
       JobIter it;
-      bool more = it.valid(p);
+      bool more = true;
       uint32_t k = 0;                   // chunks consumed
       uint32_t jobs[2] = {0u, 0u};      // jobs issued per slot
       while (more && ok) {
@@ -531,8 +539,10 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         }
         pptc::fence_after_sync();
         const uint32_t d = tmem + (uint32_t)T * p.slot_cols;
-        const uint32_t a_base = pptc::smem_u32(smem + (size_t)T * p.act_bytes);
-        const uint32_t a_sbo = (uint32_t)(K / 8) * 128u;
+        // descriptors advance by adding the byte offset / 16 to the start
+        // address field (shared addresses < 256 KB: the field never carries)
+        const uint64_t a_desc = pptc::smem_desc(pptc::smem_u32(smem + (size_t)T * p.act_bytes), 128,
+                                                (uint32_t)(K / 8) * 128u);
         const uint32_t idesc = pptc::idesc_bf16(128, N);
         for (int j = 0; j * kChunkK < K; ++j, ++k) {
           const uint32_t slot = k % kRingSlots, use = k / kRingSlots;
@@ -542,15 +552,14 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           }
           pptc::fence_after_sync();
           const int w = chunk_width(K, j);
-          const uint32_t b_base = pptc::smem_u32(ring + slot * kSlotBytes);
-          const uint32_t b_sbo = (uint32_t)(w / 8) * 128u;
-          for (int s = 0; s < w / 16; ++s) {
-            const uint64_t ad = pptc::smem_desc(a_base + (uint32_t)(j * (kChunkK / 16) + s) * 256u,
-                                                128, a_sbo);
-            const uint64_t bd = pptc::smem_desc(b_base + (uint32_t)s * 256u, 128, b_sbo);
-            pptc::mma_bf16(d, ad, bd, idesc, j > 0 || s > 0);
-          }
-          pptc::mma_commit(&w_empty[slot]);  // the slot is free once these MMAs complete
+          const uint64_t b_desc =
+              pptc::smem_desc(pptc::smem_u32(ring + slot * kSlotBytes), 128, (uint32_t)(w / 8) * 128u);
+          const uint64_t a_j = a_desc + (uint64_t)(j * (kChunkK / 16) * 16);  // + j * 64 cols * 2 B / 16
+          for (int s = 0; s < w / 16; ++s)
+            pptc::mma_bf16(d, a_j + (uint64_t)(s * 16), b_desc + (uint64_t)(s * 16), idesc,
+                           j > 0 || s > 0);
+          // the slot is free (in every CTA's view) once these MMAs complete
+          pptc::mma_commit_multicast(&w_empty[slot], (uint16_t)((1u << kCluster) - 1u));
         }
         if (!ok) break;
         pptc::mma_commit(&acc_full[T]);
@@ -572,13 +581,12 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     const int r = quad * 32 + lane;
     // first tiles of both slots
     for (int T = 0; T < 2; ++T) {
-      const int tile = (int)blockIdx.x * 2 + T;
-      if (tile < p.n_tiles) pack_input(p, smem + (size_t)T * p.act_bytes, tile, t);
+      pack_input(p, smem + (size_t)T * p.act_bytes, (int)blockIdx.x * 2 + T, t);
       pptc::fence_async_smem();
       pptc::mbar_arrive(&act_ready[T]);
     }
     JobIter it;
-    bool more = it.valid(p);
+    bool more = true;
     uint32_t jobs[2] = {0u, 0u};
     while (more) {
       const int T = it.slot, l = it.layer;
@@ -590,7 +598,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       jobs[T]++;
       pptc::fence_after_sync();
       const uint32_t trow = tmem + (uint32_t)T * p.slot_cols + ((uint32_t)(quad * 32) << 16);
-      const float* bias = sBias + l * p.hidden;
+      const float* __restrict__ bias = p.P + p.off_b[l];  // L1-resident
       if (l < p.n_layers) {
         // two 32-column slices per load-wait (columns c0 and c0 + 128)
         for (int c0 = cgrp * 32; c0 < p.hidden; c0 += 256) {
@@ -606,8 +614,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               if (cb + q * 8 >= p.hidden) break;
-              const float4 b0 = *reinterpret_cast<const float4*>(bias + cb + q * 8);
-              const float4 b1 = *reinterpret_cast<const float4*>(bias + cb + q * 8 + 4);
+              const float4 b0 = __ldg(reinterpret_cast<const float4*>(bias + cb + q * 8));
+              const float4 b1 = __ldg(reinterpret_cast<const float4*>(bias + cb + q * 8 + 4));
               const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
               union {
                 uint4 u4;
@@ -627,17 +635,21 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         // head: every epilogue warp takes the 32-column slices cgrp and
         // cgrp + 4 of its 32 rows; row maximum and normaliser are combined
         // across the four column groups in shared memory
-        const int tile = it.tile(p);
+        const int tile = it.tile();
         const long long row0 = (long long)tile * 128;
         const long long row = row0 + r;
         const int ld = p.n_bins + 1;  // odd stride: the 32 rows of a warp hit 32 banks
         float* stage = reinterpret_cast<float*>(act);
+        // row max / sum per column group, at the end of the slot's buffer
+        float(*s_max)[128] = reinterpret_cast<float(*)[128]>(act + p.act_bytes - kRedBytes);
+        float(*s_sum)[128] = s_max + 4;
         // the slot's next input, loaded now so that its latency overlaps the head
         const int next = tile + 2 * (int)gridDim.x;
         const int units = 16 * p.in_pad;  // 128 rows x in_pad / 8 chunks of 8
         const bool prefetch = units <= kEpiThreads;
         float xin[8];
-        if (prefetch && t < units && next < p.n_tiles) load_unit(p, next, t, xin);
+        const bool more_rounds = it.round + 1 < p.n_rounds;
+        if (prefetch && t < units && more_rounds) load_unit(p, next, t, xin);
         // pass 1: the log count and this warp's part of the row maximum
         float o0 = 0.0f, mx = -INFINITY;
 #pragma unroll 1
@@ -648,8 +660,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
 #pragma unroll
           for (int i = 0; i < 32; ++i) {
             const int c = sl * 32 + i;
-            if (c == 0) o0 = __uint_as_float(v[i]) + bias[0];
-            else if (c <= p.n_bins) mx = fmaxf(mx, __uint_as_float(v[i]) + bias[c]);
+            if (c == 0) o0 = __uint_as_float(v[i]) + __ldg(bias);
+            else if (c <= p.n_bins) mx = fmaxf(mx, __uint_as_float(v[i]) + __ldg(bias + c));
           }
         }
         if (cgrp == 0 && row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
@@ -669,7 +681,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
             for (int i = 0; i < 32; ++i) {
               const int c = sl * 32 + i;
               if (c >= 1 && c <= p.n_bins) {
-                const float e = __expf(__uint_as_float(v[i]) + bias[c] - mx);
+                const float e = __expf(__uint_as_float(v[i]) + __ldg(bias + c) - mx);
                 se += e;
                 if (p.stage_pdf) stage[r * ld + c - 1] = e;
               }
@@ -700,13 +712,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
                 const int c = sl * 32 + i;
                 if (c >= 1 && c <= p.n_bins && row < p.n)
                   p.pdf[row * p.n_bins + c - 1] =
-                      __expf(__uint_as_float(v[i]) + bias[c] - mx) * inv;
+                      __expf(__uint_as_float(v[i]) + __ldg(bias + c) - mx) * inv;
               }
             }
           }
         }
         epi_sync();  // the slot's buffer is read out before the next input lands
-        if (next < p.n_tiles) {
+        if (more_rounds) {
           if (prefetch) {
             if (t < units) store_unit(p, act, t, xin);
           } else {
@@ -723,6 +735,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   }
   pptc::fence_before_sync();
   __syncthreads();
+  cluster_sync();  // no copy or commit of the peer targets this CTA any more
   if (warp == 0) pptc::tmem_dealloc(tmem, 2 * p.slot_cols);
   if (threadIdx.x == 0 && (abort_flag || !ok)) atomicOr(p.err, 1u);
 }
@@ -781,6 +794,8 @@ struct pp_mlp {
   std::vector<long long> wpack_off;     // bytes per layer
   bool pack_dirty = true;
   int num_sms = 0;
+  int infer_clusters = 0;  // co-resident clusters of the inference kernel
+  size_t infer_smem = 0;
   long long step = 0;
   float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f, time_weight = 1.0f;
 };
@@ -902,20 +917,20 @@ int mlp_repack(pp_mlp* m, cudaStream_t s) {
 }
 
 // Shared memory of infer_kernel: the activations of two tiles (128 rows x
-// max(in_pad, hidden) BF16 each), the weight ring, then the biases.  The
-// head stages a tile's PDF rows (128 x (n_bins + 1) floats) in that tile's
-// activation buffer when they fit.
+// max(in_pad, hidden) BF16 each, at least the head's reduction arrays), then
+// the weight ring.  The head stages a tile's PDF rows (128 x (n_bins + 1)
+// floats) in that tile's activation buffer when they fit before the
+// reduction arrays at its end.
 struct InferSmem {
-  uint32_t act, ring_off, bias_off, total;
+  uint32_t act, ring_off, total;
   bool stage_pdf;
 };
 InferSmem infer_smem(const pp_mlp* m) {
-  const size_t act = (size_t)128 * std::max(m->hidden, m->in_pad) * 2;
+  const size_t act = std::max<size_t>((size_t)128 * std::max(m->hidden, m->in_pad) * 2, kRedBytes);
   const size_t ring_off = 2 * act;
-  const size_t bias_off = ring_off + (size_t)kRingSlots * kSlotBytes;
-  const size_t bias = sizeof(float) * ((size_t)m->n_layers * m->hidden + m->out_pad);
-  return {(uint32_t)act, (uint32_t)ring_off, (uint32_t)bias_off, (uint32_t)(bias_off + bias),
-          (size_t)128 * (m->n_bins + 1) * 4 <= act};
+  return {(uint32_t)act, (uint32_t)ring_off,
+          (uint32_t)(ring_off + (size_t)kRingSlots * kSlotBytes),
+          (size_t)128 * (m->n_bins + 1) * 4 + kRedBytes <= act};
 }
 
 int check_err(pp_mlp* m, cudaStream_t s) {
@@ -1183,7 +1198,7 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
   p.n_tiles = (int)tiles;
   p.slot_cols = 32;
   while (p.slot_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.slot_cols *= 2;
-  p.act_bytes = sm.act; p.ring_off = sm.ring_off; p.bias_off = sm.bias_off;
+  p.act_bytes = sm.act; p.ring_off = sm.ring_off;
   p.stage_pdf = sm.stage_pdf ? 1 : 0;
   p.wpack = m->wpack; p.P = m->P;
   for (int l = 0; l <= m->n_layers; ++l) {
@@ -1195,8 +1210,34 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
     e = cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device);
     if (e != cudaSuccess) return cuda_fail(e, "SM count");
   }
-  const long long grid = std::min<long long>(m->num_sms, (tiles + 1) / 2);
-  infer_kernel<<<(unsigned)grid, kInferThreads, smem, s>>>(p);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kInferThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (m->infer_clusters == 0 || m->infer_smem != smem) {
+    cfg.gridDim = dim3((unsigned)(kCluster * ((m->num_sms + kCluster - 1) / kCluster)));
+    int nc = 0;
+    e = cudaOccupancyMaxActiveClusters(&nc, infer_kernel, &cfg);
+    if (e != cudaSuccess) return cuda_fail(e, "cluster occupancy");
+    if (nc < 1) return fail(PP_ERR_CUDA, "inference kernel: no cluster fits an SM pair");
+    m->infer_clusters = nc;
+    m->infer_smem = smem;
+  }
+  // clusters co-resident at once, each with two tiles per CTA per round
+  const long long clusters =
+      std::min<long long>(m->infer_clusters, (tiles + 2 * kCluster - 1) / (2 * kCluster));
+  const long long grid = clusters * kCluster;
+  p.n_rounds = (int)((tiles + 2 * grid - 1) / (2 * grid));
+  cfg.gridDim = dim3((unsigned)grid);
+  e = cudaLaunchKernelEx(&cfg, infer_kernel, p);
+  if (e != cudaSuccess) return cuda_fail(e, "infer kernel");
   e = cudaGetLastError();
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "infer kernel");
 }
