@@ -353,27 +353,32 @@ struct InferParams {
   unsigned* err;
 };
 
-// The sequence of jobs every role walks through in the same order: rounds of
-// two tiles (slot 0 and slot 1 of this CTA), each round all layers, the two
-// slots alternating per layer, so that the tensor core works on one slot
-// while the epilogue warps drain the other.  Every CTA runs the same number
-// of rounds (the CTAs of a cluster consume one shared weight stream); tiles
-// past the last row are evaluated on zero rows and not stored.
+// The sequence of jobs every role walks through in the same order.  A CTA
+// works on two tiles at a time (slots 0 and 1), the slots alternating job by
+// job so that the tensor core works on one while the epilogue warps drain the
+// other; slot 1 runs (n_layers + 1) / 2 layers behind slot 0, so that the long
+// head epilogue of one slot overlaps a hidden layer's MMAs of the other.
+// Each slot evaluates n_rounds tiles (round r: tile (r * gridDim.x +
+// blockIdx.x) * 2 + slot); every CTA runs the same number of rounds (the
+// CTAs of a cluster consume one shared weight stream), and tiles past the
+// last row are evaluated on zero rows and not stored.
 struct JobIter {
-  int round = 0, layer = 0, slot = 0;
+  int step = -1, slot = 0, layer = 0, round = 0;
   __device__ int tile() const { return (round * (int)gridDim.x + (int)blockIdx.x) * 2 + slot; }
   // advance to the next job; false when the CTA's work is done
   __device__ bool next(const InferParams& p) {
-    if (slot == 0) {
-      slot = 1;
-      return true;
+    const int per_tile = p.n_layers + 1;
+    const int lag = per_tile / 2;
+    while (true) {
+      ++step;
+      slot = step & 1;
+      const int q = (step >> 1) - (slot ? lag : 0);
+      if (q < 0) continue;
+      round = q / per_tile;
+      layer = q - round * per_tile;
+      if (round < p.n_rounds) return true;
+      if (slot == 1) return false;  // slot 1 finishes last
     }
-    slot = 0;
-    if (++layer > p.n_layers) {
-      layer = 0;
-      if (++round >= p.n_rounds) return false;
-    }
-    return true;
   }
 };
 
@@ -483,7 +488,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     if (lane == 0) {
       const uint32_t rank = cluster_rank();
       JobIter it;
-      bool more = true;
+      bool more = it.next(p);
       uint32_t k = 0;  // chunks of the shared stream seen
       while (more && ok) {
         const int l = it.layer;
@@ -526,7 +531,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     // ---------------- MMA issuer
     if (lane == 0) {
       JobIter it;
-      bool more = true;
+      bool more = it.next(p);
       uint32_t k = 0;                   // chunks consumed
       uint32_t jobs[2] = {0u, 0u};      // jobs issued per slot
       while (more && ok) {
@@ -586,11 +591,19 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       pptc::mbar_arrive(&act_ready[T]);
     }
     JobIter it;
-    bool more = true;
+    bool more = it.next(p);
     uint32_t jobs[2] = {0u, 0u};
     while (more) {
       const int T = it.slot, l = it.layer;
       unsigned char* act = smem + (size_t)T * p.act_bytes;
+      // this lane's bias values of the job's two column slices, loaded before
+      // the wait (the inner loops broadcast them by shuffle)
+      const float* __restrict__ bias = p.P + p.off_b[l];
+      const int width = l < p.n_layers ? p.hidden : p.out_pad;
+      const int s0 = cgrp * 32;
+      const int s1 = l < p.n_layers ? cgrp * 32 + 128 : (cgrp + 4) * 32;
+      const float bl0 = s0 + lane < width ? __ldg(bias + s0 + lane) : 0.0f;
+      const float bl1 = s1 + lane < width ? __ldg(bias + s1 + lane) : 0.0f;
       if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, kWaitNs))) {
         ok = false;
         break;
@@ -598,7 +611,6 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       jobs[T]++;
       pptc::fence_after_sync();
       const uint32_t trow = tmem + (uint32_t)T * p.slot_cols + ((uint32_t)(quad * 32) << 16);
-      const float* __restrict__ bias = p.P + p.off_b[l];  // L1-resident
       if (l < p.n_layers) {
         // two 32-column slices per load-wait (columns c0 and c0 + 128)
         for (int c0 = cgrp * 32; c0 < p.hidden; c0 += 256) {
@@ -614,9 +626,10 @@ __global__ void __launch_bounds__(kInferThreads, 1)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               if (cb + q * 8 >= p.hidden) break;
-              const float4 b0 = __ldg(reinterpret_cast<const float4*>(bias + cb + q * 8));
-              const float4 b1 = __ldg(reinterpret_cast<const float4*>(bias + cb + q * 8 + 4));
-              const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+              const float blh = h ? bl1 : bl0;
+              float bb[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) bb[j] = __shfl_sync(0xffffffffu, blh, q * 8 + j);
               union {
                 uint4 u4;
                 __nv_bfloat162 h2[4];
@@ -657,11 +670,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           uint32_t v[32];
           pptc::tmem_ld32_nowait(trow + (uint32_t)(sl * 32), v);
           pptc::tmem_wait();
+          const float bsl = sl == cgrp ? bl0 : bl1;
 #pragma unroll
           for (int i = 0; i < 32; ++i) {
             const int c = sl * 32 + i;
-            if (c == 0) o0 = __uint_as_float(v[i]) + __ldg(bias);
-            else if (c <= p.n_bins) mx = fmaxf(mx, __uint_as_float(v[i]) + __ldg(bias + c));
+            const float z = __uint_as_float(v[i]) + __shfl_sync(0xffffffffu, bsl, i);
+            if (c == 0) o0 = z;
+            else if (c <= p.n_bins) mx = fmaxf(mx, z);
           }
         }
         if (cgrp == 0 && row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
@@ -677,11 +692,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
             uint32_t v[32];
             pptc::tmem_ld32_nowait(trow + (uint32_t)(sl * 32), v);
             pptc::tmem_wait();
+            const float bsl = sl == cgrp ? bl0 : bl1;
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
               const int c = sl * 32 + i;
+              const float bc = __shfl_sync(0xffffffffu, bsl, i);
               if (c >= 1 && c <= p.n_bins) {
-                const float e = __expf(__uint_as_float(v[i]) + __ldg(bias + c) - mx);
+                const float e = __expf(__uint_as_float(v[i]) + bc - mx);
                 se += e;
                 if (p.stage_pdf) stage[r * ld + c - 1] = e;
               }
@@ -707,12 +724,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
               uint32_t v[32];
               pptc::tmem_ld32_nowait(trow + (uint32_t)(sl * 32), v);
               pptc::tmem_wait();
+              const float bsl = sl == cgrp ? bl0 : bl1;
 #pragma unroll
               for (int i = 0; i < 32; ++i) {
                 const int c = sl * 32 + i;
+                const float bc = __shfl_sync(0xffffffffu, bsl, i);
                 if (c >= 1 && c <= p.n_bins && row < p.n)
-                  p.pdf[row * p.n_bins + c - 1] =
-                      __expf(__uint_as_float(v[i]) + __ldg(bias + c) - mx) * inv;
+                  p.pdf[row * p.n_bins + c - 1] = __expf(__uint_as_float(v[i]) + bc - mx) * inv;
               }
             }
           }
