@@ -422,6 +422,30 @@ __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* 
   }
 }
 
+// Bias + SiLU of one 32-column slice (columns cb .. cb + 31 of this thread's
+// row) into the BF16 activations; bl2 holds bias / 2 of column cb + lane.
+// kFull: all 32 columns exist (no bound checks, fully interleavable).
+template <bool kFull>
+__device__ __forceinline__ void silu_slice(const uint32_t* v, float bl2, int cb, int hidden,
+                                           unsigned char* act, int r) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (!kFull && cb + q * 8 >= hidden) break;
+    union {
+      uint4 u4;
+      __nv_bfloat162 h2[4];
+    } o;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int i = q * 8 + 2 * j;
+      const float h0 = fmaf(__uint_as_float(v[i]), 0.5f, __shfl_sync(0xffffffffu, bl2, i));
+      const float h1 = fmaf(__uint_as_float(v[i + 1]), 0.5f, __shfl_sync(0xffffffffu, bl2, i + 1));
+      o.h2[j] = __floats2bfloat162_rn(pptc::silu_half(h0), pptc::silu_half(h1));
+    }
+    *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, hidden)) = o.u4;
+  }
+}
+
 __device__ __forceinline__ void epi_sync() {
   asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
 }
@@ -623,25 +647,9 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           for (int h = 0; h < 2; ++h) {
             if (h == 1 && !two) break;
             const int cb = c0 + h * 128;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              if (cb + q * 8 >= p.hidden) break;
-              const float blh = h ? bl1 : bl0;
-              float bb[8];
-#pragma unroll
-              for (int j = 0; j < 8; ++j) bb[j] = __shfl_sync(0xffffffffu, blh, q * 8 + j);
-              union {
-                uint4 u4;
-                __nv_bfloat162 h2[4];
-              } o;
-#pragma unroll
-              for (int j = 0; j < 4; ++j)
-                o.h2[j] = __floats2bfloat162_rn(
-                    pptc::silu(__uint_as_float(v[h][q * 8 + 2 * j]) + bb[2 * j]),
-                    pptc::silu(__uint_as_float(v[h][q * 8 + 2 * j + 1]) + bb[2 * j + 1]));
-              *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, p.hidden)) =
-                  o.u4;
-            }
+            const float bl2 = 0.5f * (h ? bl1 : bl0);
+            if (cb + 32 <= p.hidden) silu_slice<true>(v[h], bl2, cb, p.hidden, act, r);
+            else silu_slice<false>(v[h], bl2, cb, p.hidden, act, r);
           }
         }
       } else {

@@ -183,7 +183,10 @@ __device__ __forceinline__ void tmem_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
+// silu(z) = z sigmoid(z) = h + h tanh(h) with h = z / 2 (two FMA-pipe
+// operations around the SFU one)
+__device__ __forceinline__ float silu_half(float h) { return fmaf(h, tanh_approx(h), h); }
+__device__ __forceinline__ float silu(float z) { return silu_half(0.5f * z); }
 __device__ __forceinline__ float silu_grad(float z) {
   const float s = sigmoid(z);
   return s * (1.0f + z * (1.0f - s));
