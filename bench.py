@@ -165,14 +165,20 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def profile_traffic():
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+def profile_value(key):
+    """A figure of the committed ncu summary of the propagation kernel
+    (`key: value` lines), if present."""
     try:
         text = open(PROFILE_SUMMARY).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_launch_full:\s*([0-9.eE+]+)", text)
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", text)
     return float(m.group(1)) if m else None
+
+
+def profile_traffic():
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    return profile_value("dram_bytes_per_launch_full")
 
 
 def cpu_baseline(pp, orc, config, seconds, photons_full):
@@ -542,7 +548,7 @@ def run_ours(args):
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      "traffic": traffic_full,
-                     "issue_active_frac_ncu": 0.826,
+                     "issue_active_frac_ncu": profile_value("issue_active_frac"),
                      "note": f"{FLOPS_PER_STEP} algorithmic FP32 ops per photon step x "
                              f"{steps_taken / args.steps:.4g} steps per launch (device counter); "
                              "peak = measured FFMA throughput of this GPU (pp_measure_fp32_peak)"},
