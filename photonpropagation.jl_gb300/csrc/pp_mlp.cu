@@ -69,129 +69,194 @@ __host__ __device__ inline uint32_t tmem_cols_for(int n) {
   return c;
 }
 
-// Stage rows [row0, row0 + rows_tile) x columns [k0, k0 + kKC) of an operand into
-// the core-matrix layout; rows >= rows_valid and columns >= k_end are zero.
-__device__ void stage_operand(unsigned char* dst, const bf16* __restrict__ src, long long ld,
-                              int trans, int row0, int rows_valid, int rows_tile, int k0,
-                              int k_end) {
-  constexpr int kb_n = kKC / 8;
-  if (!trans) {
-    const int nchunks = rows_tile * kb_n;
-    for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
-      const int r = c / kb_n, kb = c % kb_n;
-      const int gk = k0 + kb * 8;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (r < rows_valid && gk < k_end)
-        v = __ldg(reinterpret_cast<const uint4*>(src + (long long)(row0 + r) * ld + gk));
-      *reinterpret_cast<uint4*>(dst + pptc::core_offset(r, kb, kKC)) = v;
-    }
-  } else {
-    const int nchunks = (rows_tile / 8) * kKC;
-    for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
-      const int k = c % kKC, rg = c / kKC;
-      const int gk = k0 + k, r0 = rg * 8;
-      union {
-        uint4 u;
-        bf16 h[8];
-      } v;
-      v.u = make_uint4(0u, 0u, 0u, 0u);
-      if (gk < k_end) {
-        const bf16* p = src + (long long)gk * ld + row0 + r0;
-        if (r0 + 8 <= rows_valid) {
-          v.u = __ldg(reinterpret_cast<const uint4*>(p));
-        } else {
-          for (int j = 0; j < 8; ++j)
-            if (r0 + j < rows_valid) v.h[j] = p[j];
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 8; ++j)
-        *reinterpret_cast<bf16*>(dst + pptc::core_offset(r0 + j, k >> 3, kKC) + (k & 7) * 2) =
-            v.h[j];
-    }
+// ---------------------------------------------------------------------------
+// Training GEMM.  One CTA computes a kTileM x (<= kTileN) tile of
+// D = A * B^T over at most kGemmStages * kKC of K (longer reductions are split
+// over blockIdx.z and accumulated atomically).  Every K stage of both operands
+// is requested at once with 16-byte cp.async copies straight into the tensor
+// core's core-matrix layout (no register round trip, zero-filled past the
+// edges); the MMAs of a stage are issued as soon as it lands.
+//
+// Shared-memory tile of R rows (M or N) x kKC columns of K, 8 x 8 core matrices
+// of 128 bytes, core matrix (r / 8, k / 8) at ((r / 8) * (kKC / 8) + k / 8) * 128:
+//   K-major  (operand stored row-major over K): row r%8 at +16 (r%8), k%8 at +2 (k%8);
+//   MN-major (operand stored with R contiguous, a_trans / b_trans): k%8 at +16 (k%8),
+//            r%8 at +2 (r%8), and the instruction descriptor's transpose bit set.
+// Without swizzling both use the descriptor's LBO for the stride between core
+// matrices along K (128 B) and SBO for the stride along R (1024 B).  Either
+// way a 16-byte piece (8 consecutive elements of the contiguous dimension) is
+// one contiguous 16-byte row of a core matrix, and a K step of 16 advances the
+// descriptor by 256 bytes.
+constexpr int kTileN = 128;
+constexpr int kGemmStages = 4;                       // K <= 256 per CTA
+constexpr uint32_t kTileBytes = 128u * kKC * 2u;     // one operand tile of one stage
+constexpr uint32_t kStageBytes = 2u * kTileBytes;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_pending(int n) {  // n in 0..kGemmStages-1
+  switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
   }
 }
 
-// One CTA: a 128-row tile of D = A * B^T over the K range of blockIdx.z,
-// accumulated by tcgen05.mma in TMEM, then the fused epilogue.
+// Request rows [r0, r0 + rows_tile) x K [k0, k0 + kKC) of one operand.
+__device__ __forceinline__ void stage_async(uint32_t dst, const bf16* __restrict__ src,
+                                            long long ld, int trans, int r0, int rows_valid,
+                                            int rows_tile, int k0, int kend) {
+  const int pieces = rows_tile * (kKC / 8);
+  for (int c = threadIdx.x; c < pieces; c += blockDim.x) {
+    uint32_t off, bytes;
+    const bf16* g;
+    if (!trans) {  // piece = row r, K elements 8 kb .. 8 kb + 7
+      const int r = c >> 3, kb = c & 7;
+      const int k = k0 + kb * 8;
+      const bool in = r < rows_valid && k < kend;
+      off = (uint32_t)(((r >> 3) * (kKC / 8) + kb) * 128 + (r & 7) * 16);
+      g = in ? src + (long long)(r0 + r) * ld + k : src;
+      bytes = in ? 16u : 0u;
+    } else {       // piece = K element k, rows 8 g .. 8 g + 7
+      const int k = c % kKC, gr = c / kKC;
+      const int left = rows_valid - gr * 8;
+      const bool in = k0 + k < kend && left > 0;
+      off = (uint32_t)((gr * (kKC / 8) + (k >> 3)) * 128 + (k & 7) * 16);
+      g = in ? src + (long long)(k0 + k) * ld + r0 + gr * 8 : src;
+      bytes = in ? (uint32_t)(left >= 8 ? 16 : 2 * left) : 0u;
+    }
+    cp_async16(dst + off, g, bytes);
+  }
+}
+
 __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constant__ GemmParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
-  unsigned char* sA = smem;
-  unsigned char* sB = smem + kTileM * kKC * 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kTileM;
+  const int n0 = blockIdx.y * kTileN;
+  const int nt = min(kTileN, p.N - n0);  // multiple of 16
   const int kbeg = blockIdx.z * p.k_per_split;
   const int kend = min(p.K, kbeg + p.k_per_split);
-  const uint32_t ncols = tmem_cols_for(p.N);
+  const int nk = (kend - kbeg + kKC - 1) / kKC;  // <= kGemmStages
+  const uint32_t ncols = tmem_cols_for(nt);
+  const uint32_t s0 = pptc::smem_u32(smem);
 
+  for (int st = 0; st < nk; ++st) {
+    const int k0 = kbeg + st * kKC;
+    stage_async(s0 + st * kStageBytes, p.A, p.lda, p.a_trans, m0, min(kTileM, p.M - m0), kTileM,
+                k0, kend);
+    stage_async(s0 + st * kStageBytes + kTileBytes, p.B + (p.b_trans ? n0 : (long long)n0 * p.ldb),
+                p.ldb, p.b_trans, 0, nt, nt, k0, kend);
+    cp_async_commit();
+  }
   if (warp == 0) pptc::tmem_alloc(&tmem_slot, ncols);
   if (threadIdx.x == 0) pptc::mbar_init(&bar, 1);
   pptc::fence_before_sync();
   __syncthreads();
   pptc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = pptc::idesc_bf16(kTileM, p.N);
-  const uint32_t sbo = (kKC / 8) * 128;
+  const uint32_t idesc = pptc::idesc_bf16(kTileM, nt) | ((uint32_t)(p.a_trans != 0) << 15) |
+                         ((uint32_t)(p.b_trans != 0) << 16);
 
-  bool ok = true;
-  uint32_t phase = 0;
-  for (int k0 = kbeg; k0 < kend; k0 += kKC) {
-    stage_operand(sA, p.A, p.lda, p.a_trans, m0, min(kTileM, p.M - m0), kTileM, k0, kend);
-    stage_operand(sB, p.B, p.ldb, p.b_trans, 0, p.N, p.N, k0, kend);
+  for (int st = 0; st < nk; ++st) {
+    cp_async_wait_pending(nk - 1 - st);  // this thread's copies of stage st have landed
     pptc::fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
       pptc::fence_after_sync();
+      const uint32_t sa = s0 + st * kStageBytes, sb = sa + kTileBytes;
+      const int k0 = kbeg + st * kKC;
       for (int s = 0; s < kKC / 16 && k0 + s * 16 < kend; ++s) {
-        const uint64_t ad = pptc::smem_desc(pptc::smem_u32(sA) + s * 256, 128, sbo);
-        const uint64_t bd = pptc::smem_desc(pptc::smem_u32(sB) + s * 256, 128, sbo);
-        pptc::mma_bf16(tmem, ad, bd, idesc, k0 > kbeg || s > 0);
+        const uint64_t ad = pptc::smem_desc(sa + s * 256, 128, 1024);
+        const uint64_t bd = pptc::smem_desc(sb + s * 256, 128, 1024);
+        pptc::mma_bf16(tmem, ad, bd, idesc, st > 0 || s > 0);
       }
-      pptc::mma_commit(&bar);
     }
-    ok = pptc::mbar_wait(&bar, phase, kWaitNs);
-    phase ^= 1u;
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
   }
+  if (threadIdx.x == 0) pptc::mma_commit(&bar);
+  bool ok = nk > 0 ? pptc::mbar_wait(&bar, 0, kWaitNs) : true;
+  ok = __syncthreads_and(ok);
   pptc::fence_after_sync();
 
-  if (ok && kend > kbeg) {
+  if (ok && nk > 0) {
     const int row = m0 + warp * 32 + lane;
     const bool row_ok = row < p.M;
-    for (int c0 = 0; c0 < p.N; c0 += 32) {
+    for (int c0 = 0; c0 < nt; c0 += 32) {
       float v[32];
       pptc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
       if (!row_ok) continue;
-#pragma unroll 4
-      for (int i = 0; i < 32; ++i) {
-        const int col = c0 + i;
-        if (col >= p.N) break;
-        const float acc = v[i];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int col = n0 + c0 + q * 8;  // 8 columns per 16-byte group
+        if (c0 + q * 8 >= nt) break;
+        const float* a8 = v + q * 8;
         switch (p.mode) {
-          case kStoreF32:
-            p.C32[(long long)row * p.ldc + col] = acc + (p.bias ? p.bias[col] : 0.0f);
+          case kStoreF32: {
+            float4 lo = make_float4(a8[0], a8[1], a8[2], a8[3]);
+            float4 hi = make_float4(a8[4], a8[5], a8[6], a8[7]);
+            if (p.bias) {
+              const float4 b0 = __ldg(reinterpret_cast<const float4*>(p.bias + col));
+              const float4 b1 = __ldg(reinterpret_cast<const float4*>(p.bias + col + 4));
+              lo.x += b0.x; lo.y += b0.y; lo.z += b0.z; lo.w += b0.w;
+              hi.x += b1.x; hi.y += b1.y; hi.z += b1.z; hi.w += b1.w;
+            }
+            float4* d = reinterpret_cast<float4*>(p.C32 + (long long)row * p.ldc + col);
+            d[0] = lo;
+            d[1] = hi;
             break;
+          }
           case kHiddenFwd: {
-            const float z = acc + p.bias[col];
-            p.Z16[(long long)row * p.ldz + col] = __float2bfloat16(z);
-            p.C16[(long long)row * p.ldc16 + col] = __float2bfloat16(pptc::silu(z));
+            const float4 b0 = __ldg(reinterpret_cast<const float4*>(p.bias + col));
+            const float4 b1 = __ldg(reinterpret_cast<const float4*>(p.bias + col + 4));
+            const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            union {
+              uint4 u4;
+              __nv_bfloat162 h2[4];
+            } z16, y16;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const float za = a8[2 * j] + bb[2 * j], zb = a8[2 * j + 1] + bb[2 * j + 1];
+              z16.h2[j] = __floats2bfloat162_rn(za, zb);
+              y16.h2[j] = __floats2bfloat162_rn(pptc::silu(za), pptc::silu(zb));
+            }
+            *reinterpret_cast<uint4*>(p.Z16 + (long long)row * p.ldz + col) = z16.u4;
+            *reinterpret_cast<uint4*>(p.C16 + (long long)row * p.ldc16 + col) = y16.u4;
             break;
           }
           case kBackwardDx: {
-            const float z = __bfloat162float(p.Zprev[(long long)row * p.ldzp + col]);
-            p.C16[(long long)row * p.ldc16 + col] = __float2bfloat16(acc * pptc::silu_grad(z));
+            union {
+              uint4 u4;
+              __nv_bfloat162 h2[4];
+            } zp, o;
+            zp.u4 = __ldg(reinterpret_cast<const uint4*>(p.Zprev + (long long)row * p.ldzp + col));
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const float2 z = __bfloat1622float2(zp.h2[j]);
+              o.h2[j] = __floats2bfloat162_rn(a8[2 * j] * pptc::silu_grad(z.x),
+                                              a8[2 * j + 1] * pptc::silu_grad(z.y));
+            }
+            *reinterpret_cast<uint4*>(p.C16 + (long long)row * p.ldc16 + col) = o.u4;
             break;
           }
-          default:
-            atomicAdd(p.C32 + (long long)row * p.ldc + col, acc);
+          default: {
+            float4* d = reinterpret_cast<float4*>(p.C32 + (long long)row * p.ldc + col);
+            atomicAdd(d, make_float4(a8[0], a8[1], a8[2], a8[3]));
+            atomicAdd(d + 1, make_float4(a8[4], a8[5], a8[6], a8[7]));
             break;
+          }
         }
       }
     }
   }
+  cp_async_wait_pending(0);  // nothing in flight when shared memory is released
   pptc::fence_before_sync();
   __syncthreads();
   if (warp == 0) pptc::tmem_dealloc(tmem, ncols);
@@ -771,24 +836,20 @@ int cuda_fail(cudaError_t e, const char* what) {
   return fail(PP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// Shared memory per CTA.  Requesting at least 80 KB when the accumulator takes
-// 256 TMEM columns keeps at most two CTAs (2 x 256 = all 512 columns) on an
-// SM, so tensor-memory allocations never wait on each other.
-constexpr size_t kGemmSmemMax = 80 * 1024;
-
+// Grid: 128-row tiles x 128-column tiles x K splits of at most 256.  The
+// split size must be a multiple of kKC (except when one split covers all of K).
 cudaError_t launch_gemm(const GemmParams& p, cudaStream_t s) {
-  size_t smem = (size_t)kTileM * kKC * 2 + (size_t)p.N * kKC * 2;
-  if (tmem_cols_for(p.N) > 128) smem = std::max(smem, kGemmSmemMax);
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kGemmSmemMax);
+                                         (int)(kGemmStages * kStageBytes));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   const int splits = (p.K + p.k_per_split - 1) / p.k_per_split;
-  dim3 grid((p.M + kTileM - 1) / kTileM, 1, splits);
-  gemm_kernel<<<grid, kGemmThreads, smem, s>>>(p);
+  const int stages = std::min(kGemmStages, (p.k_per_split + kKC - 1) / kKC);
+  dim3 grid((p.M + kTileM - 1) / kTileM, (p.N + kTileN - 1) / kTileN, splits);
+  gemm_kernel<<<grid, kGemmThreads, stages * kStageBytes, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -880,7 +941,7 @@ int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cu
   loss_kernel<<<(B + 7) / 8, 256, 0, s>>>(m->O, m->out_pad, B, d_count, d_hist, m->n_bins,
                                           1.0f / (float)B, m->time_weight, m->dO16, m->dO32,
                                           m->out_pad, m->out_pad, m->loss);
-  const int ksplit = 512;
+  const int ksplit = kGemmStages * kKC;
   auto colsum16 = [&](const bf16* X, int cols, long long ld, float* out) {
     dim3 g((cols + 31) / 32, std::min(64, (B + 7) / 8));
     colsum_kernel<bf16><<<g, 256, 0, s>>>(X, B, cols, ld, out);
@@ -1301,6 +1362,10 @@ PP_API int pp_mlp_gemm_test(const void* d_a, int64_t lda, int32_t a_trans, const
   p.B = (const bf16*)d_b; p.ldb = ldb; p.b_trans = b_trans;
   p.M = M; p.N = N; p.K = K;
   p.k_per_split = k_split > 0 ? ((K + k_split - 1) / k_split + kKC - 1) / kKC * kKC : K;
+  if (p.k_per_split > kGemmStages * kKC) {
+    cudaFree(err);
+    return fail(PP_ERR_INVALID, "gemm test: at most 256 of K per split");
+  }
   p.mode = k_split > 0 ? kAccumulateF32 : kStoreF32;
   p.C32 = d_c; p.ldc = ldc; p.err = err;
   e = launch_gemm(p, (cudaStream_t)stream);

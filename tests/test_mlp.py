@@ -64,7 +64,8 @@ def test_bf16_rounding_helper():
 @pytest.mark.gpu
 @pytest.mark.parametrize("M,N,K,a_trans,b_trans,k_split", [
     (128, 256, 256, 0, 0, 0), (300, 80, 256, 0, 0, 0), (200, 16, 80, 0, 0, 0),
-    (256, 256, 1024, 1, 1, 4), (80, 256, 512, 1, 1, 2), (129, 64, 64, 0, 1, 0)])
+    (256, 256, 1024, 1, 1, 4), (80, 256, 512, 1, 1, 2), (129, 64, 64, 0, 1, 0),
+    (200, 96, 192, 1, 0, 0), (136, 144, 256, 1, 1, 0), (8192, 256, 256, 0, 0, 0)])
 def test_tcgen05_gemm(pp, gpu_ctx, M, N, K, a_trans, b_trans, k_split):
     torch = pytest.importorskip("torch")
     g = torch.Generator().manual_seed(M * 7 + N + K)
