@@ -371,6 +371,55 @@ PP_API int pp_mlp_gemm_test(const void* d_a, int64_t lda, int32_t a_trans, const
                             int64_t ldb, int32_t b_trans, int32_t M, int32_t N, int32_t K,
                             int32_t k_split, float* d_c, int64_t ldc, void* stream);
 
+/* ---- photon hits -> PMT hits (make_hits_from_photons, calc_pe_weight!) ---- */
+
+#define PP_PMT_HOMOGENEOUS 0   /* detected with probability active_area / (4 pi r^2) */
+#define PP_PMT_POM 1           /* 16-PMT optical module, POMAcceptance               */
+#define PP_POM_MAX_KNOTS 128
+
+/* One module as the detection step sees it (target i of the propagation is
+ * module_index i + 1 of its hit records). */
+typedef struct pp_pmt_target {
+  float position[3];
+  float radius;
+  int32_t kind;            /* PP_PMT_*                                        */
+  float active_area;       /* m^2, PP_PMT_HOMOGENEOUS                          */
+} pp_pmt_target;
+
+/* The POM model (src/pom.jl:16-34,63-160): PMT directions in the detector
+ * frame (the reference's pmt_coordinates after the module orientation),
+ * PMT groups (1 or 2), per-group Rayleigh widths of the angular acceptance and
+ * total acceptance vs wavelength (assets/pmt_acc.hd5), and the relative
+ * quantum efficiency vs wavelength (assets/PMTAcc.csv).  Knots ascending. */
+typedef struct pp_pom_model {
+  int32_t n_acc;
+  int32_t n_qe;
+  float acc_wavelength[PP_POM_MAX_KNOTS];
+  float acc_group1[PP_POM_MAX_KNOTS];
+  float acc_group2[PP_POM_MAX_KNOTS];
+  float sigma_group1;
+  float sigma_group2;
+  float qe_wavelength[PP_POM_MAX_KNOTS];
+  float qe[PP_POM_MAX_KNOTS];
+  float pmt_dir[16][3];
+  int32_t pmt_group[16];
+} pp_pom_model;
+
+/* Detection of n photon hits (device hit records as the propagation writes
+ * them): d_pmt_id[i] = 1-based PMT index, 0 = not detected; d_qe_weight[i]
+ * (may be NULL) = relative quantum efficiency at the hit's wavelength (the
+ * factor calc_pe_weight! multiplies into total_weight; 1 for homogeneous
+ * modules).  Replaces the per-module host loops of make_hits_from_photons
+ * (src/processing.jl:88-139) with check_pmt_hit (src/pom.jl:246-305,
+ * src/detection.jl:57-84) and calc_pe_weight! (src/processing.jl:179-205);
+ * random numbers from a Philox stream keyed on `seed` (the reference draws
+ * from Julia's global RNG).  Asynchronous on `stream`; `targets` and `pom`
+ * are host structs copied before the call returns. */
+PP_API int pp_make_hits_from_photons(const pp_hit_record* d_records, int64_t n,
+                                     const pp_pmt_target* targets, int32_t n_targets,
+                                     const pp_pom_model* pom, int64_t seed, int32_t* d_pmt_id,
+                                     float* d_qe_weight, void* stream);
+
 /* ---- diagnostics (no reference counterpart) -------------------------------- */
 
 /* Philox4x32-10 on the device: out[4*i..4*i+3] = philox(ctr[i], key), n rows.

@@ -21,6 +21,7 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
 from .targets import HomogeneousDetector, Spherical
-from . import surrogate, workloads
+from . import pom, surrogate, workloads
+from .pom import POM, calc_pe_weight, make_hits_from_photons
 
 __all__ = [n for n in dir() if not n.startswith("_")]

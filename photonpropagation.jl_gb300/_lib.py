@@ -69,6 +69,27 @@ class pp_tuning(Structure):
     ]
 
 
+PP_PMT_HOMOGENEOUS = 0
+PP_PMT_POM = 1
+PP_POM_MAX_KNOTS = 128
+
+
+class pp_pmt_target(Structure):
+    _fields_ = [("position", c_float * 3), ("radius", c_float), ("kind", c_int32),
+                ("active_area", c_float)]
+
+
+class pp_pom_model(Structure):
+    _fields_ = [
+        ("n_acc", c_int32), ("n_qe", c_int32),
+        ("acc_wavelength", c_float * PP_POM_MAX_KNOTS), ("acc_group1", c_float * PP_POM_MAX_KNOTS),
+        ("acc_group2", c_float * PP_POM_MAX_KNOTS), ("sigma_group1", c_float),
+        ("sigma_group2", c_float), ("qe_wavelength", c_float * PP_POM_MAX_KNOTS),
+        ("qe", c_float * PP_POM_MAX_KNOTS), ("pmt_dir", (c_float * 3) * 16),
+        ("pmt_group", c_int32 * 16),
+    ]
+
+
 class pp_hit_record(Structure):
     _fields_ = [
         ("position", c_float * 3), ("wavelength", c_float),
@@ -173,6 +194,8 @@ SIGNATURES = {
                                    c_void_p]),
     "pp_autotune": (c_int32, [c_void_p, c_int64, c_int32, c_int64, POINTER(pp_tuning),
                               POINTER(c_double)]),
+    "pp_make_hits_from_photons": (c_int32, [c_void_p, c_int64, POINTER(pp_pmt_target), c_int32,
+                                            c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "pp_debug_philox": (c_int32, [POINTER(c_uint32), c_int32, c_uint32, c_uint32,
                                   POINTER(c_uint32)]),
     "pp_measure_fp32_peak": (c_int32, [c_int32, POINTER(c_double)]),

@@ -1,0 +1,178 @@
+// pp_pmt.cu -- photon hits -> PMT hits on the device: the detection step that
+// follows propagation in the reference (make_hits_from_photons and
+// calc_pe_weight!, src/processing.jl:88-205), one thread per hit record.
+//
+// For a POM (src/pom.jl:246-305, POMAcceptance): with rel = (hit - centre) / r,
+// for each of the 16 PMTs (unit vector p_i, group g_i)
+//   pt_i  = acos(clamp(rel . p_i, -1, 1))
+//   w_i   = Rayleigh_{sigma_g}(pt_i) / (sin(pt_i) / 2)   (0 where sin(pt_i) = 0)
+//   prob_i = w_i * acc_g(wavelength) / 8
+// the photon is detected when u1 < sum_i prob_i, by PMT i chosen with
+// probability prob_i / sum (the first i whose running sum reaches u2 * sum).
+// acc_g and the relative quantum efficiency are linear interpolations that
+// are 0 outside their tables (Interpolations.jl, extrapolation_bc = 0).
+// For a homogeneous module (src/detection.jl:57-84) the photon is detected
+// when u1 < active_area / (4 pi r^2), as PMT 1.
+// u1, u2 are Philox4x32-10 uniforms of counter (hit index, 0x504d5400, 0),
+// key = seed, so a CPU restatement can replay every decision.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "pp_device.cuh"
+#include "pp_internal.h"
+
+namespace {
+
+constexpr int kPomPmts = 16;
+constexpr uint32_t kPmtStream = 0x504d5400u;  // Philox counter word that tags this stream
+
+struct PmtArgs {
+  const pp_hit_record* rec;
+  long long n;
+  const pp_pmt_target* targets;
+  int n_targets;
+  const pp_pom_model* pom;  // device copy, may be null
+  uint32_t key0, key1;
+  int32_t* pmt_id;
+  float* qe_weight;         // may be null
+};
+
+// Linear interpolation on ascending knots, 0 outside [x[0], x[n-1]].
+__device__ __forceinline__ float interp0(const float* x, const float* y, int n, float v) {
+  if (n < 2 || !(v >= x[0]) || !(v <= x[n - 1])) return 0.0f;
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (x[mid] <= v) lo = mid;
+    else hi = mid;
+  }
+  const float t = (v - x[lo]) / (x[hi] - x[lo]);
+  return fmaf(t, y[hi] - y[lo], y[lo]);
+}
+
+__device__ __forceinline__ float rayleigh_pdf(float x, float sigma) {
+  const float s2 = sigma * sigma;
+  return x / s2 * expf(-x * x / (2.0f * s2));
+}
+
+__global__ void pmt_kernel(const PmtArgs a) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float4* r = reinterpret_cast<const float4*>(a.rec + i);
+    const float4 pw = __ldg(r);
+    const int module = __float_as_int(__ldg(r + 4).x);  // 1-based
+    int id = 0;
+    float qe = 0.0f;
+    if (module >= 1 && module <= a.n_targets) {
+      const pp_pmt_target t = a.targets[module - 1];
+      const uint4 u = ppdev::philox(make_uint4((uint32_t)i, (uint32_t)((unsigned long long)i >> 32),
+                                            kPmtStream, 0u),
+                                 a.key0, a.key1);
+      const float u1 = ppdev::u01(u.x), u2 = ppdev::u01(u.y);
+      if (t.kind == PP_PMT_HOMOGENEOUS) {
+        const float frac = t.active_area / (4.0f * 3.14159265358979f * t.radius * t.radius);
+        id = u1 < frac ? 1 : 0;
+        qe = 1.0f;
+      } else if (t.kind == PP_PMT_POM && a.pom) {
+        const pp_pom_model& m = *a.pom;
+        const float inv_r = 1.0f / t.radius;
+        const float rx = (pw.x - t.position[0]) * inv_r;
+        const float ry = (pw.y - t.position[1]) * inv_r;
+        const float rz = (pw.z - t.position[2]) * inv_r;
+        const float acc1 = interp0(m.acc_wavelength, m.acc_group1, m.n_acc, pw.w);
+        const float acc2 = interp0(m.acc_wavelength, m.acc_group2, m.n_acc, pw.w);
+        float prob[kPomPmts];
+        float total = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kPomPmts; ++k) {
+          const float c = rx * m.pmt_dir[k][0] + ry * m.pmt_dir[k][1] + rz * m.pmt_dir[k][2];
+          const float pt = acosf(fminf(fmaxf(c, -1.0f), 1.0f));
+          const bool g1 = m.pmt_group[k] == 1;
+          const float s = sinf(pt);
+          const float w = s != 0.0f ? rayleigh_pdf(pt, g1 ? m.sigma_group1 : m.sigma_group2) / (0.5f * s)
+                                    : 0.0f;
+          prob[k] = w * (g1 ? acc1 : acc2) * 0.125f;
+          total += prob[k];
+        }
+        if (u1 < total) {
+          const float target = u2 * total;
+          float cum = 0.0f;
+          id = kPomPmts;
+#pragma unroll
+          for (int k = 0; k < kPomPmts; ++k) {
+            cum += prob[k];
+            if (cum >= target) {
+              id = k + 1;
+              break;
+            }
+          }
+        }
+        qe = interp0(m.qe_wavelength, m.qe, m.n_qe, pw.w);
+      }
+    }
+    a.pmt_id[i] = id;
+    if (a.qe_weight) a.qe_weight[i] = qe;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+PP_API int pp_make_hits_from_photons(const pp_hit_record* d_records, int64_t n,
+                                     const pp_pmt_target* targets, int32_t n_targets,
+                                     const pp_pom_model* pom, int64_t seed, int32_t* d_pmt_id,
+                                     float* d_qe_weight, void* stream) {
+  if (n < 0 || (n > 0 && (!d_records || !d_pmt_id)) || n_targets < 0 ||
+      (n_targets > 0 && !targets))
+    return pp::report_error(PP_ERR_INVALID, "pp_make_hits_from_photons: bad arguments");
+  if (pom && (pom->n_acc < 2 || pom->n_acc > PP_POM_MAX_KNOTS || pom->n_qe < 2 ||
+              pom->n_qe > PP_POM_MAX_KNOTS))
+    return pp::report_error(PP_ERR_INVALID, "pp_make_hits_from_photons: bad POM tables");
+  for (int i = 0; i < n_targets; ++i) {
+    if (targets[i].kind == PP_PMT_POM && !pom)
+      return pp::report_error(PP_ERR_INVALID, "pp_make_hits_from_photons: POM target without model");
+    if (!(targets[i].radius > 0.0f))
+      return pp::report_error(PP_ERR_INVALID, "pp_make_hits_from_photons: target radius <= 0");
+  }
+  if (n == 0) return PP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t tb = sizeof(pp_pmt_target) * (size_t)(n_targets > 0 ? n_targets : 1);
+  const size_t pb = pom ? sizeof(pp_pom_model) : 0;
+  unsigned char* buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&buf, tb + pb, s);
+  if (e == cudaSuccess && n_targets > 0)
+    e = cudaMemcpyAsync(buf, targets, sizeof(pp_pmt_target) * n_targets, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && pom) e = cudaMemcpyAsync(buf + tb, pom, pb, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) {
+    if (buf) cudaFreeAsync(buf, s);
+    return pp::report_error(PP_ERR_CUDA,
+                            std::string("pp_make_hits_from_photons: ") + cudaGetErrorString(e));
+  }
+  PmtArgs a{};
+  a.rec = d_records;
+  a.n = n;
+  a.targets = reinterpret_cast<const pp_pmt_target*>(buf);
+  a.n_targets = n_targets;
+  a.pom = pom ? reinterpret_cast<const pp_pom_model*>(buf + tb) : nullptr;
+  a.key0 = (uint32_t)(uint64_t)seed;
+  a.key1 = (uint32_t)((uint64_t)seed >> 32);
+  a.pmt_id = d_pmt_id;
+  a.qe_weight = d_qe_weight;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long blocks = std::min<long long>((n + 255) / 256, (long long)sms * 8);
+  pmt_kernel<<<(unsigned)blocks, 256, 0, s>>>(a);
+  e = cudaGetLastError();
+  cudaFreeAsync(buf, s);
+  if (e != cudaSuccess)
+    return pp::report_error(PP_ERR_CUDA,
+                            std::string("pp_make_hits_from_photons: ") + cudaGetErrorString(e));
+  return PP_OK;
+}
+
+}  // extern "C"
