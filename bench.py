@@ -64,10 +64,10 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-c2", action="store_true", help="skip the C2 batched-launch report")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the C3/C4 surrogate report")
-    ap.add_argument("--c3-pairs", type=float, default=5e5,
-                    help="training pairs of the C3 report (the full table is 2e6)")
-    ap.add_argument("--c3-steps", type=int, default=6000)
+    ap.add_argument("--c3-pairs", type=float, default=2e6, help="training pairs of the C3 report")
+    ap.add_argument("--c3-steps", type=int, default=20000)
     ap.add_argument("--c4-pairs", type=float, default=1e6)
+    ap.add_argument("--no-detection", action="store_true", help="skip the PMT detection report")
     ap.add_argument("--surrogate-only", action="store_true",
                     help="print only the C3/C4 surrogate report (for profiling its kernels)")
     return ap.parse_args()
@@ -403,6 +403,93 @@ def bench_surrogate(pp, torch, local, args):
     }
 
 
+def bench_detection(pp, torch, local, n=100_000_000, reps=5):
+    """Photon hits -> PMT hits (pp_make_hits_from_photons) on 1e8 synthetic hit
+    records on 400 POMs at the C1 module positions (positions uniform on the
+    module surfaces, wavelengths with density 1/lambda^2 on 300-800 nm),
+    device-resident;
+    8 GB of records, so every launch streams from HBM."""
+    import ctypes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pmt_oracle
+    pom = pp.pom
+    det, _ = pp.workloads.detector_400()
+    targets = [pom.POM.at(t.shape.position, t.module_id) for t in det]
+    centres = torch.tensor(np.array([t.shape.position for t in targets], np.float32),
+                           device="cuda")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    rec = torch.zeros((n, 20), dtype=torch.float32, device="cuda")  # 80-byte records
+    mi = torch.randint(0, len(targets), (n,), device="cuda", generator=g)
+    v = torch.randn((n, 3), device="cuda", generator=g)
+    v /= v.norm(dim=1, keepdim=True)
+    rec[:, 0:3] = centres[mi] + pom.POM_RADIUS * v
+    del v
+    u = torch.rand(n, device="cuda", generator=g)
+    rec[:, 3] = 1.0 / (1.0 / 300.0 - u * (1.0 / 300.0 - 1.0 / 800.0))  # density 1/lambda^2
+    del u
+    rec[:, 16] = (mi + 1).to(torch.int32).view(torch.float32)
+    ids = torch.empty(n, dtype=torch.int32, device="cuda")
+    qe = torch.empty(n, dtype=torch.float32, device="cuda")
+    tg = pom.pmt_targets(targets)
+    model = pom.pom_model()
+    lib = pp._lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def launch(seed):
+        pp._lib.check(lib.pp_make_hits_from_photons(ctypes.c_void_p(rec.data_ptr()), n, tg,
+                                                    len(targets), ctypes.byref(model), seed,
+                                                    ctypes.c_void_p(ids.data_ptr()),
+                                                    ctypes.c_void_p(qe.data_ptr()),
+                                                    ctypes.c_void_p(stream)))
+    for k in range(3):
+        launch(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(reps):
+        launch(10 + k)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    detected = int((ids > 0).sum().item())
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    algo = 40.0  # bytes per hit: 2 x 16 B of the record read, 4 B id + 4 B QE written
+    achieved = n * algo / (ms * 1e-3) / 1e9
+    # CPU: the numpy oracle (one thread) on a bounded sample of the same records
+    m = 2_000_000
+    host = rec[:m].cpu().numpy()
+    t = pom.load_pom_tables()
+    model_d = dict(acc_wavelength=t.acc_wavelength, acc_group1=t.acc_group1,
+                   acc_group2=t.acc_group2, sigma_group1=t.sigma_group1,
+                   sigma_group2=t.sigma_group2, qe_wavelength=t.qe_wavelength, qe=t.qe,
+                   pmt_dir=pom.pom_pmt_directions(), pmt_group=pom.POM_PMT_GROUP)
+    otargets = [dict(position=x.shape.position, radius=x.shape.radius, kind="pom",
+                     active_area=x.pmt_area) for x in targets]
+    t0 = time.perf_counter()
+    pmt_oracle.detect(host[:, 0:3], host[:, 3], host[:, 16].view(np.int32), otargets, model_d, 0)
+    cpu_rate = m / (time.perf_counter() - t0)
+    del rec, ids, qe, mi
+    torch.cuda.empty_cache()
+    return {"workload": "1e8 hit records on 400 POMs (C1 positions), uniform on the module "
+                        "surfaces, 1/lambda^2 wavelengths on 300-800 nm; records resident in "
+                        "HBM (8 GB)",
+            "hits_per_s": n / (ms * 1e-3), "ms": ms, "detected_fraction": detected / n,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm if hbm else None,
+                         "note": "40 algorithmic bytes per hit; peak = measured copy bandwidth. "
+                                 "The kernel is instruction-issue bound, not HBM-bound: each hit "
+                                 "evaluates acos, sqrt and exp2 for 16 PMTs"},
+            "cpu_baseline": {"value": cpu_rate, "unit": "hits/s", "cores": 1, "kind": "port",
+                             "sample": f"numpy oracle on the first {m} records"}}
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -516,6 +603,7 @@ def run_ours(args):
     e2e_value = e2e_photons * world / e2e_s
     c2 = None if (world > 1 or args.no_c2 or args.config != "c1") else bench_c2(pp, torch, local)
     sur = None if (world > 1 or args.no_surrogate) else bench_surrogate(pp, torch, local, args)
+    detection = None if (world > 1 or args.no_detection) else bench_detection(pp, torch, local)
 
     if rank != 0:
         return 0
@@ -560,6 +648,7 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "c2_batched": c2,
         "surrogate": sur,
+        "detection": detection,
         "wall_s_timed_region": wall,
     }
     print(json.dumps(line))

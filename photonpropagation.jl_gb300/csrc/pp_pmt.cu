@@ -14,7 +14,9 @@
 // For a homogeneous module (src/detection.jl:57-84) the photon is detected
 // when u1 < active_area / (4 pi r^2), as PMT 1.
 // u1, u2 are Philox4x32-10 uniforms of counter (hit index, 0x504d5400, 0),
-// key = seed, so a CPU restatement can replay every decision.
+// key = seed, so a CPU restatement can replay every decision (up to the
+// rounding of the arithmetic: sin(pt) is evaluated as sqrt(1 - cos^2 pt),
+// the Gaussian factor by exp2f).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,12 +55,20 @@ __device__ __forceinline__ float interp0(const float* x, const float* y, int n, 
   return fmaf(t, y[hi] - y[lo], y[lo]);
 }
 
-__device__ __forceinline__ float rayleigh_pdf(float x, float sigma) {
-  const float s2 = sigma * sigma;
-  return x / s2 * expf(-x * x / (2.0f * s2));
-}
-
-__global__ void pmt_kernel(const PmtArgs a) {
+// The POM model in shared memory (staged once per block; the grid strides).
+__global__ void __launch_bounds__(256) pmt_kernel(const PmtArgs a) {
+  __shared__ pp_pom_model sm;
+  if (a.pom) {
+    const int* src = reinterpret_cast<const int*>(a.pom);
+    int* dst = reinterpret_cast<int*>(&sm);
+    for (int w = threadIdx.x; w < (int)(sizeof(pp_pom_model) / 4); w += blockDim.x) dst[w] = src[w];
+  }
+  __syncthreads();
+  // Rayleigh(pt; sigma) = pt / sigma^2 * 2^(pt^2 * (-log2(e) / (2 sigma^2))), per group
+  const float inv_s2_1 = 1.0f / (sm.sigma_group1 * sm.sigma_group1);
+  const float inv_s2_2 = 1.0f / (sm.sigma_group2 * sm.sigma_group2);
+  const float e2_1 = -0.72134752044448170368f * inv_s2_1;  // -log2(e) / 2
+  const float e2_2 = -0.72134752044448170368f * inv_s2_2;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
        i += (long long)gridDim.x * blockDim.x) {
     const float4* r = reinterpret_cast<const float4*>(a.rec + i);
@@ -77,7 +87,7 @@ __global__ void pmt_kernel(const PmtArgs a) {
         id = u1 < frac ? 1 : 0;
         qe = 1.0f;
       } else if (t.kind == PP_PMT_POM && a.pom) {
-        const pp_pom_model& m = *a.pom;
+        const pp_pom_model& m = sm;
         const float inv_r = 1.0f / t.radius;
         const float rx = (pw.x - t.position[0]) * inv_r;
         const float ry = (pw.y - t.position[1]) * inv_r;
@@ -88,13 +98,14 @@ __global__ void pmt_kernel(const PmtArgs a) {
         float total = 0.0f;
 #pragma unroll
         for (int k = 0; k < kPomPmts; ++k) {
-          const float c = rx * m.pmt_dir[k][0] + ry * m.pmt_dir[k][1] + rz * m.pmt_dir[k][2];
-          const float pt = acosf(fminf(fmaxf(c, -1.0f), 1.0f));
+          const float c = fminf(fmaxf(rx * m.pmt_dir[k][0] + ry * m.pmt_dir[k][1] +
+                                          rz * m.pmt_dir[k][2], -1.0f), 1.0f);
+          const float pt = acosf(c);
           const bool g1 = m.pmt_group[k] == 1;
-          const float s = sinf(pt);
-          const float w = s != 0.0f ? rayleigh_pdf(pt, g1 ? m.sigma_group1 : m.sigma_group2) / (0.5f * s)
-                                    : 0.0f;
-          prob[k] = w * (g1 ? acc1 : acc2) * 0.125f;
+          const float s = sqrtf(fmaxf(1.0f - c * c, 0.0f));  // sin(acos(c)) for pt in [0, pi]
+          const float pdf = pt * (g1 ? inv_s2_1 : inv_s2_2) * exp2f(pt * pt * (g1 ? e2_1 : e2_2));
+          // w / 8 = pdf / (s / 2) / 8 = pdf / (4 s)
+          prob[k] = s != 0.0f ? __fdividef(pdf, 4.0f * s) * (g1 ? acc1 : acc2) : 0.0f;
           total += prob[k];
         }
         if (u1 < total) {
