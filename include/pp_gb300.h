@@ -237,7 +237,10 @@ PP_API int pp_total_photons(const pp_ctx* ctx, int64_t* total);
 /* Asynchronous launch on `stream` (cudaStream_t; NULL = legacy default
  * stream): zeroes *d_counters, runs the persistent propagation kernel over
  * every uploaded source, writes hits into d_hits (device memory, capacity
- * records).  The device-resident form of cuda_propagate_photons! launched
+ * records).  The pp_set_* calls of a context first wait for its launches
+ * (pp_launch, pp_launch_histogram, pp_launch_graph) still running, since
+ * they overwrite the device inputs those launches read; so a caller may
+ * upload the next batch of sources right after a launch.  The device-resident form of cuda_propagate_photons! launched
  * once per source (src/photon_prop_cuda.jl:927-943): here one launch covers
  * all sources through a device work queue. */
 PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* d_hits,

@@ -105,6 +105,9 @@ struct pp_ctx {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  // recorded after every launch on the caller's stream: setters wait on it
+  // before they overwrite device inputs that a launch in flight still reads
+  cudaEvent_t inflight = nullptr;
   unsigned long long version = 1;
 
   // medium
@@ -318,6 +321,14 @@ int validate_launch(pp_ctx* ctx, int n_steps, const void* d_hits, long long capa
 
 int fetch_hits(pp_ctx* ctx, const pp_hits* out, long long n);
 
+// Block until the context's launches on callers' streams have finished.
+void wait_launches(pp_ctx* ctx) {
+  if (ctx && ctx->inflight) cudaEventSynchronize(ctx->inflight);
+}
+void mark_launch(pp_ctx* ctx, cudaStream_t s) {
+  if (ctx->inflight) cudaEventRecord(ctx->inflight, s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -351,6 +362,7 @@ PP_API int pp_create(pp_ctx** out, int32_t device) {
   ctx->device = device;
   e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->inflight, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_ctr, sizeof(pp_counters));
   if (e != cudaSuccess) {
     int rc = cuda_error(e, "pp_create");
@@ -365,6 +377,7 @@ PP_API int pp_create(pp_ctx** out, int32_t device) {
 PP_API int pp_destroy(pp_ctx* ctx) {
   if (!ctx) return PP_OK;
   DeviceScope ds(ctx->device);
+  wait_launches(ctx);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   cudaFree(ctx->d_medium);
@@ -380,11 +393,13 @@ PP_API int pp_destroy(pp_ctx* ctx) {
   cudaFree(ctx->d_ctr);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->inflight) cudaEventDestroy(ctx->inflight);
   delete ctx;
   return PP_OK;
 }
 
 PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !m) return set_error(PP_ERR_INVALID, "null argument");
   if (m->n_knots < 2 || !(m->wl_step > 0.0f) || !std::isfinite(m->wl_min))
     return set_error(PP_ERR_INVALID, "medium grid needs n_knots >= 2 and wl_step > 0");
@@ -431,6 +446,7 @@ PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
 }
 
 PP_API int pp_set_spectrum(pp_ctx* ctx, const float* knots, int32_t n) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !knots || n < 1) return set_error(PP_ERR_INVALID, "spectrum needs n >= 1 knots");
   for (int i = 0; i < n; ++i)
     if (!(knots[i] > 0.0f) || !std::isfinite(knots[i]))
@@ -448,6 +464,7 @@ PP_API int pp_set_spectrum(pp_ctx* ctx, const float* knots, int32_t n) {
 }
 
 PP_API int pp_set_monochromatic(pp_ctx* ctx, float wavelength) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !(wavelength > 0.0f) || !std::isfinite(wavelength))
     return set_error(PP_ERR_INVALID, "monochromatic wavelength must be positive");
   DeviceScope ds(ctx->device);
@@ -461,6 +478,7 @@ PP_API int pp_set_monochromatic(pp_ctx* ctx, float wavelength) {
 }
 
 PP_API int pp_set_track_smear(pp_ctx* ctx, const float* q, int32_t n) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !q || n < 2) return set_error(PP_ERR_INVALID, "track table needs n >= 2 knots");
   for (int i = 0; i < n; ++i)
     if (!(q[i] >= -1.0f && q[i] <= 1.0f))
@@ -476,6 +494,7 @@ PP_API int pp_set_track_smear(pp_ctx* ctx, const float* q, int32_t n) {
 }
 
 PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell_size) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || n < 0 || (n > 0 && !t)) return set_error(PP_ERR_INVALID, "bad target list");
   if (n > 65535) return set_error(PP_ERR_INVALID, "at most 65535 targets are supported");
   for (int i = 0; i < n; ++i) {
@@ -503,6 +522,7 @@ PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell
 }
 
 PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float photon_scaling) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || n < 0 || (n > 0 && !s)) return set_error(PP_ERR_INVALID, "bad source list");
   if (!(photon_scaling >= 0.0f) || !std::isfinite(photon_scaling))
     return set_error(PP_ERR_INVALID, "photon_scaling must be finite and >= 0");
@@ -528,6 +548,7 @@ PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float phot
 }
 
 PP_API int pp_set_tuning(pp_ctx* ctx, const pp_tuning* t) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !t) return set_error(PP_ERR_INVALID, "null argument");
   if (t->block_threads < 64 || t->block_threads > 512 || (t->block_threads % 32) != 0)
     return set_error(PP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 512]");
@@ -569,7 +590,9 @@ PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* 
   int rc = validate_launch(ctx, n_steps, d_hits, capacity, d_counters);
   if (rc != PP_OK) return rc;
   DeviceScope ds(ctx->device);
-  return enqueue(ctx, seed, n_steps, d_hits, capacity, d_counters, (cudaStream_t)stream);
+  rc = enqueue(ctx, seed, n_steps, d_hits, capacity, d_counters, (cudaStream_t)stream);
+  if (rc == PP_OK) mark_launch(ctx, (cudaStream_t)stream);
+  return rc;
 }
 
 PP_API int pp_launch_histogram(pp_ctx* ctx, int64_t seed, int32_t n_steps, const float* d_tgeo,
@@ -596,6 +619,7 @@ PP_API int pp_launch_histogram(pp_ctx* ctx, int64_t seed, int32_t n_steps, const
                                        ctx->tuning.precise_math != 0, use_smem_grid(ctx),
                                        ctx->num_sms, s, nullptr);
   if (e != cudaSuccess) return cuda_error(e, "launch propagate kernel (histogram)");
+  mark_launch(ctx, s);
   return PP_OK;
 }
 
@@ -638,6 +662,7 @@ PP_API int pp_launch_graph(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_re
     ctx->gkey = key;
   }
   PP_CUDA(cudaGraphLaunch(ctx->gexec, s), "graph launch");
+  mark_launch(ctx, s);
   return PP_OK;
 }
 

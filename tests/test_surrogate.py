@@ -228,3 +228,23 @@ def test_training_checkpoint_resume(pp, gpu_ctx, tmp_path):
     assert np.linalg.norm(pa - pb) <= 1e-3 * np.linalg.norm(pa)
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+def test_tables_do_not_depend_on_chunking(pp, gpu_ctx):
+    """Chunks launched back to back (each chunk's sources uploaded while the
+    previous launch may still run) give the tables that separate, synchronised
+    runs of the same chunks give."""
+    s = pp.surrogate
+    ctx = pp.Context(0)
+    rng = np.random.default_rng(12)
+    n, chunk, photons, seed = 600, 100, 200_000, 3
+    pairs = s.Pairs(rng.uniform(5.0, 10.0, n), s._unit(rng, n), s._unit(rng, n),
+                    np.zeros(n, np.int32))
+    together, _ = s.generate_tables(pairs, photons, seed=seed, ctx=ctx, chunk=chunk)
+    apart = np.concatenate([
+        s.generate_tables(pairs.subset(slice(lo, lo + chunk)), photons, seed=seed + lo, ctx=ctx,
+                          chunk=chunk)[0] for lo in range(0, n, chunk)])
+    assert together.sum() > 1000
+    np.testing.assert_allclose(together, apart, rtol=1e-4, atol=1e-4)
+    ctx.close()
