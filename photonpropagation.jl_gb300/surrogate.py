@@ -276,9 +276,14 @@ class MLP:
 
 
 def train(mlp: MLP, x, counts, hists, steps: int, batch: int = 8192, lr: float = 1e-3,
-          seed: int = 0, log_every: int = 0):
+          seed: int = 0, log_every: int = 0, lr_final: float | None = None):
     """Adam on (features, expected hits, time histograms) held in device memory
-    (torch tensors); returns the list of (step, loss) logged."""
+    (torch tensors); returns the list of (step, loss) logged.  The step size
+    starts at `lr` and follows a cosine down to `lr_final` (default lr / 100)
+    at the last step, so that the final parameters are not those of one noisy
+    step at full rate."""
+    import math
+    lr_final = lr * 0.01 if lr_final is None else lr_final
     import torch
     n = x.shape[0]
     g = torch.Generator(device="cuda")
@@ -292,7 +297,9 @@ def train(mlp: MLP, x, counts, hists, steps: int, batch: int = 8192, lr: float =
         torch.index_select(x, 0, idx, out=bx)
         torch.index_select(counts, 0, idx, out=bc)
         torch.index_select(hists, 0, idx, out=bh)
-        mlp.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), batch, lr)
+        frac = s / max(1, steps - 1)
+        rate = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * frac))
+        mlp.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), batch, rate)
         if log_every and (s % log_every == 0 or s == steps - 1):
             log.append((s, mlp.last_loss()))
     return log
