@@ -423,6 +423,13 @@ PP_API int pp_make_hits_from_photons(const pp_hit_record* d_records, int64_t n,
                                      const pp_pom_model* pom, int64_t seed, int32_t* d_pmt_id,
                                      float* d_qe_weight, void* stream);
 
+/* Time residuals of n device hit records: d_tres[i] = time - tgeo[module] - t0
+ * (NaN for a module index outside [1, n_targets]), tgeo the host array of
+ * per-target geometric times (calc_tgeo / calc_tgeo_tracks for the first
+ * source).  The per-hit part of calc_time_residual! (src/calc.jl:270-323). */
+PP_API int pp_time_residuals(const pp_hit_record* d_records, int64_t n, const double* tgeo,
+                             int32_t n_targets, double t0, double* d_tres, void* stream);
+
 /* ---- diagnostics (no reference counterpart) -------------------------------- */
 
 /* Philox4x32-10 on the device: out[4*i..4*i+3] = philox(ctr[i], key), n rows.

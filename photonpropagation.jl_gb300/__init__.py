@@ -21,7 +21,9 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
 from .targets import HomogeneousDetector, Spherical
-from . import pom, surrogate, workloads
+from . import calc, pom, surrogate, workloads
+from .calc import (calc_tgeo, calc_tgeo_tracks, calc_time_residual, closest_approach_distance,
+                   closest_approach_param)
 from .pom import POM, calc_pe_weight, make_hits_from_photons
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -196,6 +196,8 @@ SIGNATURES = {
                               POINTER(c_double)]),
     "pp_make_hits_from_photons": (c_int32, [c_void_p, c_int64, POINTER(pp_pmt_target), c_int32,
                                             c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "pp_time_residuals": (c_int32, [c_void_p, c_int64, POINTER(c_double), c_int32, c_double,
+                                    c_void_p, c_void_p]),
     "pp_debug_philox": (c_int32, [POINTER(c_uint32), c_int32, c_uint32, c_uint32,
                                   POINTER(c_uint32)]),
     "pp_measure_fp32_peak": (c_int32, [c_int32, POINTER(c_double)]),

@@ -129,9 +129,45 @@ __global__ void __launch_bounds__(256) pmt_kernel(const PmtArgs a) {
   }
 }
 
+__global__ void tres_kernel(const pp_hit_record* __restrict__ rec, long long n,
+                            const double* __restrict__ tgeo, int n_targets, double t0,
+                            double* __restrict__ tres) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int module = rec[i].module_index;  // 1-based
+    tres[i] = module >= 1 && module <= n_targets ? rec[i].time - tgeo[module - 1] - t0
+                                                 : __longlong_as_double(0x7ff8000000000000ll);
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+PP_API int pp_time_residuals(const pp_hit_record* d_records, int64_t n, const double* tgeo,
+                             int32_t n_targets, double t0, double* d_tres, void* stream) {
+  if (n < 0 || (n > 0 && (!d_records || !d_tres)) || n_targets < 0 || (n_targets > 0 && !tgeo))
+    return pp::report_error(PP_ERR_INVALID, "pp_time_residuals: bad arguments");
+  if (n == 0) return PP_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* d_tg = nullptr;
+  const size_t tb = sizeof(double) * (size_t)(n_targets > 0 ? n_targets : 1);
+  cudaError_t e = cudaMallocAsync((void**)&d_tg, tb, s);
+  if (e == cudaSuccess && n_targets > 0)
+    e = cudaMemcpyAsync(d_tg, tgeo, sizeof(double) * n_targets, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long blocks = std::min<long long>((n + 255) / 256, (long long)sms * 8);
+    tres_kernel<<<(unsigned)blocks, 256, 0, s>>>(d_records, n, d_tg, n_targets, t0, d_tres);
+    e = cudaGetLastError();
+  }
+  if (d_tg) cudaFreeAsync(d_tg, s);
+  if (e != cudaSuccess)
+    return pp::report_error(PP_ERR_CUDA, std::string("pp_time_residuals: ") + cudaGetErrorString(e));
+  return PP_OK;
+}
 
 PP_API int pp_make_hits_from_photons(const pp_hit_record* d_records, int64_t n,
                                      const pp_pmt_target* targets, int32_t n_targets,
