@@ -453,3 +453,94 @@ class Surrogate:
                     pdf[rest] = self._normalise(mc_h)
                 from_mc[rest] = True
         return Expectations(counts, pdf, from_mc, stats)
+
+
+# ---------------------------------------------------------------------------
+# Table files.
+
+class TableStore:
+    """Append-only store of surrogate tables: a directory of parts
+    ``part_00001.npz``, ``part_00002.npz``, ... each holding one batch of pairs
+    (distance, module_dir, emitter_dir, spectrum_id), their counts and
+    histograms, and the batch's attributes (photons, seed, ...).  The
+    append-with-counter pattern of the reference's save_hdf! (group,
+    dataset_k, nsims; scripts/photon_tables/utils.jl:24-56) -- without HDF5,
+    which needs h5py, absent here -- so a table run can be resumed batch by
+    batch (generate_tables is deterministic per batch and seed)."""
+
+    def __init__(self, path: str):
+        import os
+        self.path = path
+        os.makedirs(path, exist_ok=True)
+
+    @property
+    def nsims(self) -> int:
+        import os
+        return sum(1 for f in os.listdir(self.path) if f.startswith("part_") and f.endswith(".npz"))
+
+    def append(self, pairs: Pairs, counts, hists, **attrs) -> str:
+        import json
+        import os
+        k = self.nsims + 1
+        fname = os.path.join(self.path, f"part_{k:05d}.npz")
+        np.savez(fname, distance=pairs.distance, module_dir=pairs.module_dir,
+                 emitter_dir=pairs.emitter_dir, spectrum_id=pairs.spectrum_id,
+                 counts=np.asarray(counts, np.float32), hists=np.asarray(hists, np.float32),
+                 attrs=np.array(json.dumps(attrs)))
+        return fname
+
+    def read(self):
+        """(Pairs, counts, hists, [attrs per part]) of all parts in order."""
+        import json
+        import os
+        parts = sorted(f for f in os.listdir(self.path) if f.startswith("part_"))
+        zs = [np.load(os.path.join(self.path, f)) for f in parts]
+        if not zs:
+            return Pairs(np.zeros(0), np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0, np.int32)), \
+                np.zeros(0, np.float32), np.zeros((0, N_BINS), np.float32), []
+        cat = lambda k: np.concatenate([z[k] for z in zs])  # noqa: E731
+        pairs = Pairs(cat("distance"), cat("module_dir"), cat("emitter_dir"), cat("spectrum_id"))
+        return pairs, cat("counts"), cat("hists"), [json.loads(str(z["attrs"])) for z in zs]
+
+
+def write_arrow(path: str, pairs: Pairs, counts, hists, **attrs) -> None:
+    """Arrow IPC file of a table (one row per pair: distance, module and
+    emitter directions, spectrum id, count, histogram; attributes in the
+    schema metadata), the format of the reference's photon_table_for_sr.jl
+    writer (scripts/photon_tables/photon_table_for_sr.jl:214-224).  Needs
+    pyarrow."""
+    import json
+
+    import pyarrow as pa
+    n = len(pairs)
+    cols = {
+        "distance": pa.array(pairs.distance, pa.float64()),
+        "module_dir": pa.FixedSizeListArray.from_arrays(
+            pa.array(np.asarray(pairs.module_dir, np.float64).ravel()), 3),
+        "emitter_dir": pa.FixedSizeListArray.from_arrays(
+            pa.array(np.asarray(pairs.emitter_dir, np.float64).ravel()), 3),
+        "spectrum_id": pa.array(np.asarray(pairs.spectrum_id, np.int32)),
+        "count": pa.array(np.asarray(counts, np.float32)),
+        "hist": pa.FixedSizeListArray.from_arrays(
+            pa.array(np.asarray(hists, np.float32).reshape(n, -1).ravel()),
+            np.asarray(hists).shape[1] if n else N_BINS),
+    }
+    table = pa.table(cols).replace_schema_metadata({"attrs": json.dumps(attrs)})
+    with pa.OSFile(path, "wb") as f, pa.ipc.new_file(f, table.schema) as w:
+        w.write_table(table)
+
+
+def read_arrow(path: str):
+    """(Pairs, counts, hists, attrs) of a write_arrow file."""
+    import json
+
+    import pyarrow as pa
+    with pa.memory_map(path) as f:
+        table = pa.ipc.open_file(f).read_all()
+    n = table.num_rows
+    flat = lambda name, w: np.asarray(table.column(name).combine_chunks().flatten()).reshape(n, w)  # noqa: E731
+    pairs = Pairs(np.asarray(table.column("distance")), flat("module_dir", 3),
+                  flat("emitter_dir", 3), np.asarray(table.column("spectrum_id")))
+    hists = flat("hist", table.schema.field("hist").type.list_size)
+    attrs = json.loads(table.schema.metadata[b"attrs"].decode())
+    return pairs, np.asarray(table.column("count")), hists, attrs

@@ -248,3 +248,42 @@ def test_tables_do_not_depend_on_chunking(pp, gpu_ctx):
     assert together.sum() > 1000
     np.testing.assert_allclose(together, apart, rtol=1e-4, atol=1e-4)
     ctx.close()
+
+
+def _fake_tables(pp, n, seed):
+    s = pp.surrogate
+    rng = np.random.default_rng(seed)
+    p = s.sample_pairs(n, seed=seed)
+    return p, rng.poisson(3.0, n).astype(np.float32), rng.random((n, s.N_BINS)).astype(np.float32)
+
+
+def test_table_store_appends_and_reads_back(pp, tmp_path):
+    s = pp.surrogate
+    st = s.TableStore(str(tmp_path / "tables"))
+    assert st.nsims == 0
+    a = _fake_tables(pp, 50, 1)
+    b = _fake_tables(pp, 30, 2)
+    st.append(*a, photons=100_000, seed=1)
+    st.append(*b, photons=100_000, seed=2)
+    assert s.TableStore(str(tmp_path / "tables")).nsims == 2
+    pairs, counts, hists, attrs = st.read()
+    np.testing.assert_array_equal(pairs.distance, np.concatenate([a[0].distance, b[0].distance]))
+    np.testing.assert_array_equal(pairs.emitter_dir, np.concatenate([a[0].emitter_dir,
+                                                                     b[0].emitter_dir]))
+    np.testing.assert_array_equal(counts, np.concatenate([a[1], b[1]]))
+    np.testing.assert_array_equal(hists, np.concatenate([a[2], b[2]]))
+    assert [x["seed"] for x in attrs] == [1, 2]
+
+
+def test_arrow_tables_round_trip(pp, tmp_path):
+    pytest.importorskip("pyarrow")
+    s = pp.surrogate
+    p, c, h = _fake_tables(pp, 40, 3)
+    f = str(tmp_path / "t.arrow")
+    s.write_arrow(f, p, c, h, photons=100_000, seed=3)
+    q, c2, h2, attrs = s.read_arrow(f)
+    np.testing.assert_array_equal(q.distance, p.distance)
+    np.testing.assert_array_equal(q.module_dir, p.module_dir)
+    np.testing.assert_array_equal(c2, c)
+    np.testing.assert_array_equal(h2, h)
+    assert attrs == {"photons": 100_000, "seed": 3}
