@@ -234,6 +234,24 @@ PP_API int pp_total_photons(const pp_ctx* ctx, int64_t* total);
 
 /* ---- propagation ---------------------------------------------------------- */
 
+/* Targets of any shape (src/photon_prop_cuda.jl:345-404): spheres, and the
+ * horizontal (normal e_z) rectangle and disc of the reference's Rectangular
+ * and Circular shapes.  With any non-spherical target the kernel tests every
+ * target at every step in index order, as the reference does (no culling
+ * grid); a list of spheres only takes the culled path of pp_set_targets. */
+#define PP_TARGET_SPHERE 0
+#define PP_TARGET_RECTANGLE 1
+#define PP_TARGET_DISC 2
+typedef struct pp_target {
+  float position[3];
+  float radius;      /* sphere, disc */
+  float length_x;    /* rectangle */
+  float length_y;    /* rectangle */
+  int32_t kind;      /* PP_TARGET_* */
+  int32_t reserved;
+} pp_target;
+PP_API int pp_set_shaped_targets(pp_ctx* ctx, const pp_target* t, int32_t n);
+
 /* Asynchronous launch on `stream` (cudaStream_t; NULL = legacy default
  * stream): zeroes *d_counters, runs the persistent propagation kernel over
  * every uploaded source, writes hits into d_hits (device memory, capacity

@@ -59,7 +59,7 @@ class ppo_run(Structure):
         ("spectrum_knots", POINTER(c_float)), ("n_spectrum", c_int32),
         ("mono_wavelength", c_float),
         ("track_quantiles", POINTER(c_float)), ("n_track", c_int32), ("reserved", c_int32),
-        ("seed", c_int64),
+        ("seed", c_int64), ("shapes", c_void_p), ("n_shapes", c_int32), ("reserved2", c_int32),
     ]
 
 
@@ -151,7 +151,7 @@ class Run:
 
     def __init__(self, source_records, n_src, sphere_records, n_targets, medium_params,
                  spectrum_knots=None, mono_wavelength=0.0, track_quantiles=None, seed=1,
-                 n_steps=15, photon_scaling=1.0):
+                 n_steps=15, photon_scaling=1.0, shape_records=None):
         self.L = load()
         self._keep = [source_records, sphere_records]
         self.medium, k = make_medium(medium_params)
@@ -160,8 +160,15 @@ class Run:
         r.sources = ctypes.cast(source_records, c_void_p)
         r.n_src = n_src
         r.photon_scaling = photon_scaling
-        r.targets = ctypes.cast(sphere_records, c_void_p) if n_targets else None
-        r.n_targets = n_targets
+        if shape_records is not None:
+            self._keep.append(shape_records)
+            r.shapes = ctypes.cast(shape_records, c_void_p)
+            r.n_shapes = n_targets
+            r.targets = None
+            r.n_targets = 0
+        else:
+            r.targets = ctypes.cast(sphere_records, c_void_p) if n_targets else None
+            r.n_targets = n_targets
         r.n_steps = n_steps
         r.medium = ctypes.pointer(self.medium)
         if spectrum_knots is not None:
@@ -180,8 +187,11 @@ class Run:
 
     @classmethod
     def from_setup(cls, setup, n_steps=15):
-        return cls(setup.source_records(), len(setup.sources), setup.sphere_records(),
+        shaped = setup.has_shaped_targets()
+        return cls(setup.source_records(), len(setup.sources),
+                   None if shaped else setup.sphere_records(),
                    len(setup.targets), setup.medium.oracle_params(),
+                   shape_records=setup.target_records() if shaped else None,
                    spectrum_knots=setup.spectrum_knots,
                    mono_wavelength=setup.mono_wavelength or 0.0,
                    track_quantiles=setup.track_quantiles() if setup.needs_track_smear() else None,

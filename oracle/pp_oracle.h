@@ -91,6 +91,12 @@ typedef struct ppo_run {
   int32_t n_track;
   int32_t reserved;
   int64_t seed;
+  /* shaped targets (used instead of `targets` when n_shapes > 0): spheres,
+   * rectangles and discs tested in index order (check_intersection,
+   * src/photon_prop_cuda.jl:345-404) */
+  const pp_target* shapes;
+  int32_t n_shapes;
+  int32_t reserved2;
 } ppo_run;
 
 typedef struct ppo_stats {

@@ -20,7 +20,7 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
                       PointlikeIsotropicEmitter, PointlikeTimeRangeEmitter, source_photons)
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
-from .targets import HomogeneousDetector, Spherical
+from .targets import Circular, HomogeneousDetector, Rectangular, Spherical
 from . import calc, pom, surrogate, workloads
 from .calc import (calc_tgeo, calc_tgeo_tracks, calc_time_residual, closest_approach_distance,
                    closest_approach_param)

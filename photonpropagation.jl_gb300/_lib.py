@@ -69,6 +69,16 @@ class pp_tuning(Structure):
     ]
 
 
+PP_TARGET_SPHERE = 0
+PP_TARGET_RECTANGLE = 1
+PP_TARGET_DISC = 2
+
+
+class pp_target(Structure):
+    _fields_ = [("position", c_float * 3), ("radius", c_float), ("length_x", c_float),
+                ("length_y", c_float), ("kind", c_int32), ("reserved", c_int32)]
+
+
 PP_PMT_HOMOGENEOUS = 0
 PP_PMT_POM = 1
 PP_POM_MAX_KNOTS = 128
@@ -196,6 +206,7 @@ SIGNATURES = {
                               POINTER(c_double)]),
     "pp_make_hits_from_photons": (c_int32, [c_void_p, c_int64, POINTER(pp_pmt_target), c_int32,
                                             c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "pp_set_shaped_targets": (c_int32, [c_void_p, POINTER(pp_target), c_int32]),
     "pp_time_residuals": (c_int32, [c_void_p, c_int64, POINTER(c_double), c_int32, c_double,
                                     c_void_p, c_void_p]),
     "pp_debug_philox": (c_int32, [POINTER(c_uint32), c_int32, c_uint32, c_uint32,

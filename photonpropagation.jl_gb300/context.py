@@ -129,6 +129,9 @@ class Context:
     def set_targets(self, spheres, n: int, cell_size: float = 0.0) -> None:
         check(self._lib.pp_set_targets(self.ptr, spheres, n, float(cell_size)), "pp_set_targets")
 
+    def set_shaped_targets(self, records, n: int) -> None:
+        check(self._lib.pp_set_shaped_targets(self.ptr, records, n), "pp_set_shaped_targets")
+
     def set_sources(self, records, n: int, scaling: float = 1.0) -> None:
         check(self._lib.pp_set_sources(self.ptr, records, n, float(scaling)), "pp_set_sources")
 

@@ -130,6 +130,8 @@ struct pp_ctx {
   // targets and grid
   std::vector<pp_sphere> h_targets;
   pp_sphere* d_targets = nullptr;
+  float4* d_shapes = nullptr;  // shaped targets (then the sphere list is empty)
+  int n_shapes = 0;
   unsigned char* d_blob = nullptr;
   GridDev grid{};
   unsigned char* d_safety = nullptr;
@@ -273,6 +275,8 @@ LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_reco
   a.blob = ctx->d_blob;
   a.grid = ctx->grid;
   a.safety = ctx->d_safety;
+  a.shapes = ctx->n_shapes > 0 ? ctx->d_shapes : nullptr;
+  a.n_shapes = ctx->n_shapes;
   a.sgrid = ctx->sgrid;
   a.medium = ctx->d_medium;
   a.n_medium = ctx->n_medium;
@@ -384,6 +388,7 @@ PP_API int pp_destroy(pp_ctx* ctx) {
   cudaFree(ctx->d_spectrum);
   cudaFree(ctx->d_track);
   cudaFree(ctx->d_targets);
+  cudaFree(ctx->d_shapes);
   cudaFree(ctx->d_blob);
   cudaFree(ctx->d_safety);
   cudaFree(ctx->d_sources);
@@ -503,6 +508,9 @@ PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell
       return set_error(PP_ERR_INVALID, "target %d has a non-finite position or radius <= 0", i);
   }
   DeviceScope ds(ctx->device);
+  cudaFree(ctx->d_shapes);
+  ctx->d_shapes = nullptr;
+  ctx->n_shapes = 0;
   ctx->h_targets.assign(t, t + n);
   cudaFree(ctx->d_targets);
   ctx->d_targets = nullptr;
@@ -518,6 +526,60 @@ PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell
     return rc;
   }
   ctx->has_targets = true;
+  return PP_OK;
+}
+
+PP_API int pp_set_shaped_targets(pp_ctx* ctx, const pp_target* t, int32_t n) {
+  wait_launches(ctx);  // inputs of launches in flight are about to change
+  if (!ctx || n < 0 || (n > 0 && !t)) return set_error(PP_ERR_INVALID, "bad target list");
+  if (n > 65535) return set_error(PP_ERR_INVALID, "at most 65535 targets are supported");
+  bool spheres_only = true;
+  for (int i = 0; i < n; ++i) {
+    const pp_target& x = t[i];
+    if (!std::isfinite(x.position[0]) || !std::isfinite(x.position[1]) ||
+        !std::isfinite(x.position[2]))
+      return set_error(PP_ERR_INVALID, "target %d has a non-finite position", i);
+    if (x.kind == PP_TARGET_SPHERE || x.kind == PP_TARGET_DISC) {
+      if (!(x.radius > 0.0f) || !std::isfinite(x.radius))
+        return set_error(PP_ERR_INVALID, "target %d: radius must be > 0", i);
+    } else if (x.kind == PP_TARGET_RECTANGLE) {
+      if (!(x.length_x > 0.0f) || !(x.length_y > 0.0f) || !std::isfinite(x.length_x) ||
+          !std::isfinite(x.length_y))
+        return set_error(PP_ERR_INVALID, "target %d: rectangle lengths must be > 0", i);
+    } else {
+      return set_error(PP_ERR_INVALID, "target %d: unknown kind %d", i, x.kind);
+    }
+    spheres_only = spheres_only && x.kind == PP_TARGET_SPHERE;
+  }
+  if (spheres_only) {
+    std::vector<pp_sphere> sp(n);
+    for (int i = 0; i < n; ++i) {
+      for (int k = 0; k < 3; ++k) sp[i].position[k] = t[i].position[k];
+      sp[i].radius = t[i].radius;
+    }
+    return pp_set_targets(ctx, n ? sp.data() : nullptr, n, 0.0f);
+  }
+  // no culling grid: an empty sphere list, then the shapes
+  int rc = pp_set_targets(ctx, nullptr, 0, 0.0f);
+  if (rc != PP_OK) return rc;
+  DeviceScope ds(ctx->device);
+  std::vector<float4> h(2 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const pp_target& x = t[i];
+    const bool rect = x.kind == PP_TARGET_RECTANGLE;
+    const float p0 = rect ? 0.5f * x.length_x : x.radius * x.radius;
+    const float p1 = rect ? 0.5f * x.length_y : 0.0f;
+    int kind = x.kind;
+    float kf;
+    memcpy(&kf, &kind, sizeof(kf));
+    h[2 * i] = make_float4(x.position[0], x.position[1], x.position[2], p0);
+    h[2 * i + 1] = make_float4(p1, kf, 0.0f, 0.0f);
+  }
+  PP_CUDA(cudaMalloc(&ctx->d_shapes, sizeof(float4) * h.size()), "cudaMalloc(shaped targets)");
+  PP_CUDA(cudaMemcpy(ctx->d_shapes, h.data(), sizeof(float4) * h.size(), cudaMemcpyHostToDevice),
+          "upload shaped targets");
+  ctx->n_shapes = n;
+  ctx->version++;
   return PP_OK;
 }
 

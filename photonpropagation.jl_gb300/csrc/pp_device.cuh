@@ -265,6 +265,28 @@ __device__ __forceinline__ bool sphere_hit(float4 s, float3 pos, float3 dir, flo
   return false;
 }
 
+// Intersection with target j of a shaped-target list (check_intersection,
+// src/photon_prop_cuda.jl:345-404): spheres by the sphere formula above;
+// rectangles and discs lie in the plane z = z_j, met at d = (z_j - z) / dir_z
+// when 0 <= d <= step and the point is strictly inside the shape.
+template <bool P>
+__device__ __forceinline__ bool shape_hit(const float4* __restrict__ shapes, int j, float3 pos,
+                                          float3 dir, float step, float* d_out) {
+  const float4 g = __ldg(shapes + 2 * j);
+  const float4 h = __ldg(shapes + 2 * j + 1);
+  const int kind = __float_as_int(h.y);
+  if (kind == PP_TARGET_SPHERE) return sphere_hit<P>(g, pos, dir, step, d_out);
+  if (dir.z == 0.0f) return false;
+  const float d = f_div<P>(g.z - pos.z, dir.z);
+  if (d < 0.0f || d > step) return false;
+  const float x = madd<P>(dir.x, d, pos.x) - g.x;
+  const float y = madd<P>(dir.y, d, pos.y) - g.y;
+  const bool in = kind == PP_TARGET_RECTANGLE ? (fabsf(x) < g.w && fabsf(y) < h.x)
+                                              : (x * x + y * y < g.w);
+  if (in) *d_out = d;
+  return in;
+}
+
 // First target in index order intersected within (0, step): the candidates
 // come from a 3-D DDA walk over the uniform grid cells the segment crosses
 // (Amanatides & Woo); among all intersected candidates the smallest index

@@ -96,6 +96,10 @@ struct LaunchArgs {
   GridDev grid;
   const unsigned char* safety;             // safety field (global memory)
   SafetyDev sgrid;
+  // Shaped targets (no grid): 2 float4 per target, {x, y, z, p0} {p1, kind}:
+  // sphere p0 = r^2; rectangle p0, p1 = half lengths; disc p0 = r^2.
+  const float4* shapes;
+  int n_shapes;
 
   const float4* medium;                    // {sca_len, v_group, abs_len, n}
   int n_medium;

@@ -213,7 +213,9 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
 #define PP_PROPAGATE_MIN_BLOCKS 2
 #endif
 
-template <bool kPrecise, bool kSmemGrid>
+// kShapes: shaped targets (a.shapes), every target tested at every step in
+// index order (no grid, no deferred queue).
+template <bool kPrecise, bool kSmemGrid, bool kShapes = false>
 __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
     propagate_kernel(const __grid_constant__ LaunchArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -359,9 +361,29 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
       best.key[lane] = 0xffffffffu;
       __syncwarp();
       int count = 0;  // warp-uniform length of the deferred-segment queue
+      bool found = false;  // shaped targets: the photon has hit
       for (int k = 1; k <= a.n_steps; ++k) {
         const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.key0, a.key1);
         const float step = -f_log<kPrecise>(u01(r.x)) * sca_len;
+        if constexpr (kShapes) {
+          if (active && !found) {
+            for (int j = 0; j < a.n_shapes; ++j) {
+              float d;
+              if (shape_hit<kPrecise>(a.shapes, j, pos, dir, step, &d)) {
+                found = true;
+                best.key[lane] = ((uint32_t)k << 16) | (uint32_t)j;
+                best.hx[lane] = madd<kPrecise>(dir.x, d, pos.x);
+                best.hy[lane] = madd<kPrecise>(dir.y, d, pos.y);
+                best.hz[lane] = madd<kPrecise>(dir.z, d, pos.z);
+                best.ox[lane] = dir.x;
+                best.oy[lane] = dir.y;
+                best.oz[lane] = dir.z;
+                best.dist[lane] = (dist - comp) + d;
+                break;
+              }
+            }
+          }
+        } else {
         const bool need = have_grid && active && !segment_clear<kSmemGrid>(a.sgrid, field, pos, dir, step);
         const unsigned m = __ballot_sync(0xffffffffu, need);
         if (m) {
@@ -385,6 +407,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
           count += nn;
           __syncwarp();
         }
+        }  // kShapes
         pos = make_float3(madd<kPrecise>(dir.x, step, pos.x), madd<kPrecise>(dir.y, step, pos.y),
                           madd<kPrecise>(dir.z, step, pos.z));
         {
@@ -394,7 +417,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         }
         dir = update_direction<kPrecise>(a.phase, dir, u01(r.y), u01(r.z), u01(r.w));
       }
-      if (count > 0) drain_queue<kPrecise>(q, best, count, a.grid, cells, items, sph, lane);
+      if (!kShapes && count > 0)
+        drain_queue<kPrecise>(q, best, count, a.grid, cells, items, sph, lane);
       __syncwarp();
 
       const uint32_t key = best.key[lane];
@@ -441,9 +465,9 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
   }
 }
 
-template <bool P, bool S>
+template <bool P, bool S, bool Sh = false>
 const void* kernel_ptr() {
-  return reinterpret_cast<const void*>(&propagate_kernel<P, S>);
+  return reinterpret_cast<const void*>(&propagate_kernel<P, S, Sh>);
 }
 
 }  // namespace

@@ -8,12 +8,13 @@
 namespace pp {
 
 // Replay variant, instantiated in pp_propagate_precise.cu.
-const void* precise_kernel_ptr(bool smem_grid);
+const void* precise_kernel_ptr(bool smem_grid, bool shapes);
 
 namespace {
 
-const void* select_kernel(bool precise, bool smem_grid) {
-  if (precise) return precise_kernel_ptr(smem_grid);
+const void* select_kernel(bool precise, bool smem_grid, bool shapes = false) {
+  if (precise) return precise_kernel_ptr(smem_grid, shapes);
+  if (shapes) return kernel_ptr<false, false, true>();
   return smem_grid ? kernel_ptr<false, true>() : kernel_ptr<false, false>();
 }
 
@@ -35,7 +36,9 @@ int propagate_occupancy(int block_threads, bool precise, bool smem_tables, uint3
 cudaError_t launch_propagate(const LaunchArgs& args, int block_threads, int ctas_per_sm,
                              bool precise, bool smem_grid, int num_sms, cudaStream_t stream,
                              int* grid_out) {
-  const void* k = select_kernel(precise, smem_grid);
+  const bool shapes = args.shapes != nullptr;
+  if (shapes) smem_grid = false;
+  const void* k = select_kernel(precise, smem_grid, shapes);
   if (block_threads > kMaxBlockThreads || block_threads % 32) return cudaErrorInvalidValue;
   LaunchArgs a = args;
   const size_t smem = propagate_smem_bytes(args.grid.blob_bytes, args.sgrid.bytes, smem_grid,

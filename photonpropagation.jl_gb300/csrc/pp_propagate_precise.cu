@@ -10,7 +10,8 @@
 
 namespace pp {
 
-const void* precise_kernel_ptr(bool smem_grid) {
+const void* precise_kernel_ptr(bool smem_grid, bool shapes) {
+  if (shapes) return kernel_ptr<true, false, true>();
   return smem_grid ? kernel_ptr<true, true>() : kernel_ptr<true, false>();
 }
 

@@ -72,6 +72,12 @@ class PhotonPropSetup:
     def sphere_records(self):
         return _targets.to_spheres(self.targets)
 
+    def has_shaped_targets(self) -> bool:
+        return _targets.is_shaped(self.targets)
+
+    def target_records(self):
+        return _targets.to_targets(self.targets)
+
     def upload(self, ctx, cell_size: float = 0.0) -> None:
         """Send medium, spectrum, track table and targets to a Context."""
         ctx.set_medium(self.medium_tables())
@@ -81,4 +87,7 @@ class PhotonPropSetup:
             ctx.set_monochromatic(self.mono_wavelength)
         if self.needs_track_smear():
             ctx.set_track_smear(self.track_quantiles())
-        ctx.set_targets(self.sphere_records(), len(self.targets), cell_size)
+        if self.has_shaped_targets():
+            ctx.set_shaped_targets(self.target_records(), len(self.targets))
+        else:
+            ctx.set_targets(self.sphere_records(), len(self.targets), cell_size)
