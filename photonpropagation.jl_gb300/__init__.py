@@ -21,7 +21,9 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
 from .targets import Circular, HomogeneousDetector, Rectangular, Spherical
-from . import calc, pom, surrogate, workloads
+from . import calc, particles, pom, surrogate, workloads
+from .particles import (Particle, cascade_cherenkov_track_length, particle_shape, propagate_particles,
+                        rescale_source, split_source, total_lightyield)
 from .calc import (calc_tgeo, calc_tgeo_tracks, calc_time_residual, closest_approach_distance,
                    closest_approach_param)
 from .pom import POM, calc_pe_weight, make_hits_from_photons
