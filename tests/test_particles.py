@@ -97,4 +97,22 @@ def test_propagate_particles_pipeline(pp, gpu_ctx):
     for col in ("pmt_id", "tres", "qe_weight", "total_weight"):
         assert col in hits
     assert hits["pmt_id"].min() >= 1 and hits["pmt_id"].max() <= 16
-    assert np.all(hits["tres"] > -0.5)
+    # tres = time - tgeo(module) - t0, tgeo from the cascade vertex
+    tg = {t.module_id: pp.calc_tgeo(np.linalg.norm(t.shape.position), m, target=t)
+          for t in targets}
+    tgeo = np.array([tg[int(k)] for k in hits["module_id"]])
+    np.testing.assert_allclose(hits["tres"], hits["time"] - tgeo, atol=1e-9)
+    # causality: light leaves the axis at depth s >= 0 at time s / c (the particle
+    # outruns the light, so residuals below zero are physical) and travels at most
+    # at the largest group velocity of the spectrum
+    # (the minimum over s of s / c + |p - s e_z| / v sits where z - s = rho beta / sqrt(1 - beta^2),
+    # beta = v / c, clamped to s >= 0)
+    c = pp.medium.C_VAC_M_NS
+    v_max = max(float(m.group_velocity(wl)) for wl in np.linspace(300, 800, 501))
+    beta = v_max / c
+    pos = np.asarray(hits["position"], np.float64)
+    rho = np.hypot(pos[:, 0], pos[:, 1])
+    s = np.maximum(pos[:, 2] - rho * beta / np.sqrt(1 - beta ** 2), 0.0)
+    t_min = s / c + np.sqrt(rho ** 2 + (pos[:, 2] - s) ** 2) / v_max
+    assert np.all(hits["time"] >= t_min - 1e-3), (hits["time"] - t_min).min()
+    assert hits["tres"].min() < -1.0  # the extended emission is visible
