@@ -431,7 +431,7 @@ def bench_detection(pp, torch, local, n=100_000_000, reps=5):
     rec[:, 16] = (mi + 1).to(torch.int32).view(torch.float32)
     ids = torch.empty(n, dtype=torch.int32, device="cuda")
     qe = torch.empty(n, dtype=torch.float32, device="cuda")
-    tg = pom.pmt_targets(targets)
+    tg = pp.detection.pmt_targets(targets)
     model = pom.pom_model()
     lib = pp._lib.load()
     stream = torch.cuda.current_stream().cuda_stream

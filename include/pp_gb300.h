@@ -396,7 +396,11 @@ PP_API int pp_mlp_gemm_test(const void* d_a, int64_t lda, int32_t a_trans, const
 
 #define PP_PMT_HOMOGENEOUS 0   /* detected with probability active_area / (4 pi r^2) */
 #define PP_PMT_POM 1           /* 16-PMT optical module, POMAcceptance               */
+#define PP_PMT_DOM 2           /* single-PMT DOM, DOMAcceptance                      */
+#define PP_PMT_MULTIPMT 3      /* SphericalMultiPMTTarget (generic multi-PMT module) */
 #define PP_POM_MAX_KNOTS 128
+#define PP_DOM_MAX_POLY 16
+#define PP_MULTIPMT_MAX_PMTS 32
 
 /* One module as the detection step sees it (target i of the propagation is
  * module_index i + 1 of its hit records). */
@@ -426,6 +430,48 @@ typedef struct pp_pom_model {
   int32_t pmt_group[16];
 } pp_pom_model;
 
+/* The DOM model (src/dom.jl:8-26,96-134): an angular acceptance polynomial in
+ * the cosine of the photon direction's zenith in the module frame (coefficients
+ * in ascending powers, its maximum `polymax`) and a wavelength acceptance
+ * (assets/icecube_wl_acc.csv divided by the DOM's cross-section).
+ * zenith_axis = the third column of the module orientation, so that
+ * cos zenith = zenith_axis . direction = (inv(orientation) * direction)[3].
+ * apply_wl_acceptance = 0 skips the wavelength test (make_hits_from_photons
+ * with apply_wl_acc = false, src/processing.jl:126-128). */
+typedef struct pp_dom_model {
+  int32_t n_poly;
+  int32_t n_wl;
+  float poly[PP_DOM_MAX_POLY];
+  float polymax;
+  float zenith_axis[3];
+  int32_t apply_wl_acceptance;
+  float wl[PP_POM_MAX_KNOTS];
+  float wl_acc[PP_POM_MAX_KNOTS];
+} pp_dom_model;
+
+/* The generic multi-PMT module (src/detection.jl:90-131,
+ * src/generic_multipmt.jl): n_pmt PMTs of area pmt_area; the PMT axes in the
+ * module frame (the projected-area hit probability uses them unrotated, as the
+ * reference does) and after the module orientation (the PMT choice); the
+ * quantum efficiency vs wavelength (assets/R6091_relqe.csv, QE / 100). */
+typedef struct pp_multipmt_model {
+  int32_t n_pmt;
+  int32_t n_qe;
+  float pmt_area;
+  float pmt_dir_module[PP_MULTIPMT_MAX_PMTS][3];
+  float pmt_dir[PP_MULTIPMT_MAX_PMTS][3];
+  float qe_wavelength[PP_POM_MAX_KNOTS];
+  float qe[PP_POM_MAX_KNOTS];
+} pp_multipmt_model;
+
+/* The detection models of one call; a model may be NULL when no target has
+ * its kind. */
+typedef struct pp_detection_models {
+  const pp_pom_model* pom;
+  const pp_dom_model* dom;
+  const pp_multipmt_model* multipmt;
+} pp_detection_models;
+
 /* Detection of n photon hits (device hit records as the propagation writes
  * them): d_pmt_id[i] = 1-based PMT index, 0 = not detected; d_qe_weight[i]
  * (may be NULL) = relative quantum efficiency at the hit's wavelength (the
@@ -440,6 +486,19 @@ PP_API int pp_make_hits_from_photons(const pp_hit_record* d_records, int64_t n,
                                      const pp_pmt_target* targets, int32_t n_targets,
                                      const pp_pom_model* pom, int64_t seed, int32_t* d_pmt_id,
                                      float* d_qe_weight, void* stream);
+
+/* pp_make_hits_from_photons for every module kind: POMs as above; a DOM
+ * (check_pmt_hit and apply_wl_acceptance, src/dom.jl:96-134) is detected, as
+ * PMT 1, when u1 * polymax < poly(cos zenith) and u2 < wl_acc(wavelength),
+ * qe weight 1 (the reference defines no QE for DOMs); a multi-PMT module
+ * (check_pmt_hit, src/detection.jl:90-131) is hit when u1 <= sum over PMTs of
+ * max(direction . axis, 0) * pmt_area / (pi r^2), by the PMT that a cumulative
+ * scan of the weights -(rel . axis) picks for u2 (StatsBase 0.34 weighted
+ * sample), qe weight = QE(wavelength). */
+PP_API int pp_make_hits_from_photons_models(const pp_hit_record* d_records, int64_t n,
+                                            const pp_pmt_target* targets, int32_t n_targets,
+                                            const pp_detection_models* models, int64_t seed,
+                                            int32_t* d_pmt_id, float* d_qe_weight, void* stream);
 
 /* Time residuals of n device hit records: d_tres[i] = time - tgeo[module] - t0
  * (NaN for a module index outside [1, n_targets]), tgeo the host array of

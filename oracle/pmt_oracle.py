@@ -1,8 +1,12 @@
 """CPU ORACLE of the detection step (test infrastructure only).
 
 numpy restatement, in FP32 like the device, of photon hits -> PMT hits:
-check_pmt_hit for a POM with POMAcceptance (src/pom.jl:246-305) and for a
-homogeneous module (src/detection.jl:57-84), and the relative quantum
+check_pmt_hit for a POM with POMAcceptance (src/pom.jl:246-305), for a
+homogeneous module (src/detection.jl:57-84), for a DOM with its wavelength
+acceptance (src/dom.jl:96-134), for a generic multi-PMT module
+(src/detection.jl:90-131, the PMT drawn by StatsBase 0.34's weighted sample:
+the first index whose running weight sum reaches U * sum, else the last), and
+the quantum
 efficiency of calc_pe_weight! (src/processing.jl:179-205), drawing u1, u2 from
 the same Philox4x32-10 stream as photonpropagation.jl_gb300/csrc/pp_pmt.cu
 (counter (row, 0x504d5400, 0), key = seed) so that every decision can be
@@ -60,14 +64,64 @@ def rayleigh_pdf(x, sigma):
     return (x / s2 * np.exp(-x * x / (np.float32(2.0) * s2))).astype(np.float32)
 
 
-def detect(positions, wavelengths, module_index, targets, model, seed):
+def _dom(dirs, wl, u1, u2, m):
+    """DOM: detected (as PMT 1) when u1 * polymax < poly(cos zenith) and, with
+    the wavelength acceptance on, u2 < wl_acc(wavelength)."""
+    z = np.asarray(m["zenith_axis"], np.float32)
+    cz = (dirs.astype(np.float64) @ z.astype(np.float64)).astype(np.float32)
+    poly = np.zeros(len(cz), np.float32)
+    for c in np.asarray(m["poly"], np.float32)[::-1]:  # Horner, one rounding per step
+        poly = (poly.astype(np.float64) * cz + np.float64(c)).astype(np.float32)
+    ang = (u1 * np.float32(m["polymax"])).astype(np.float32) < poly
+    wl_ok = u2 < interp0(m["wl"], m["wl_acc"], wl) if m.get("apply_wl", True) else True
+    return np.where(ang & wl_ok, 1, 0).astype(np.int32)
+
+
+def _multipmt(pos, dirs, wl, u1, u2, centre, radius, m):
+    """Multi-PMT: hit when u1 <= sum_k max(dir . q_k, 0) * area / (pi r^2),
+    then the PMT of a cumulative scan of w_k = -(rel . p_k) for u2."""
+    qm = np.asarray(m["pmt_dir_module"], np.float32)
+    qo = np.asarray(m["pmt_dir"], np.float32)
+    n_pmt = len(qm)
+    proj = np.zeros(len(wl), np.float32)
+    for k in range(n_pmt):
+        c = (dirs[:, 0] * qm[k, 0] + dirs[:, 1] * qm[k, 1] + dirs[:, 2] * qm[k, 2]).astype(
+            np.float32)
+        proj = np.where(c > 0, (proj + c).astype(np.float32), proj)
+    prob = ((proj * np.float32(m["pmt_area"])).astype(np.float32) /
+            ((np.float32(3.14159265358979) * radius).astype(np.float32) * radius)).astype(
+        np.float32)
+    hit = u1 <= prob
+    rel = ((pos - centre) * (np.float32(1.0) / radius)).astype(np.float32)
+    w = np.stack([-(rel[:, 0] * qo[k, 0] + rel[:, 1] * qo[k, 1] + rel[:, 2] * qo[k, 2])
+                  for k in range(n_pmt)], axis=1).astype(np.float32)
+    wsum = np.zeros(len(wl), np.float32)
+    for k in range(n_pmt):
+        wsum = (wsum + w[:, k]).astype(np.float32)
+    target = (u2 * wsum).astype(np.float32)
+    chosen = np.full(len(wl), n_pmt, np.int32)
+    cw = np.zeros(len(wl), np.float32)
+    done = np.zeros(len(wl), bool)
+    for k in range(n_pmt):
+        cw = (cw + w[:, k]).astype(np.float32)
+        now = (~done) & ~(cw < target)
+        chosen[now] = k + 1
+        done |= now
+    return np.where(hit, chosen, 0).astype(np.int32), interp0(m["qe_wavelength"], m["qe"], wl)
+
+
+def detect(positions, wavelengths, module_index, targets, model, seed, directions=None):
     """PMT id per hit (0 = not detected) and the QE weight.
 
-    targets: list of dicts {position, radius, kind ('pom'|'homogeneous'),
-    active_area}; model: dict with acc_wavelength, acc_group1, acc_group2,
-    sigma_group1, sigma_group2, qe_wavelength, qe, pmt_dir (16 x 3),
-    pmt_group (16)."""
+    targets: list of dicts {position, radius, kind ('pom'|'homogeneous'|'dom'|
+    'multipmt'), active_area}; model: dict with acc_wavelength, acc_group1,
+    acc_group2, sigma_group1, sigma_group2, qe_wavelength, qe, pmt_dir (16 x 3),
+    pmt_group (16) for POMs, and sub-dicts model['dom'] (poly, polymax,
+    zenith_axis, wl, wl_acc, apply_wl) and model['multipmt'] (pmt_dir_module,
+    pmt_dir, pmt_area, qe_wavelength, qe) for those kinds; directions (n x 3)
+    are needed by DOMs and multi-PMT modules."""
     pos = np.asarray(positions, np.float32).reshape(-1, 3)
+    dirs = None if directions is None else np.asarray(directions, np.float32).reshape(-1, 3)
     wl = np.asarray(wavelengths, np.float32)
     mi = np.asarray(module_index, np.int64)
     n = len(wl)
@@ -87,6 +141,15 @@ def detect(positions, wavelengths, module_index, targets, model, seed):
                                                   radius * radius)
             ids[sel] = (u1[sel] < frac).astype(np.int32)
             qe[sel] = 1.0
+            continue
+        if t["kind"] == "dom":
+            ids[sel] = _dom(dirs[sel], wl[sel], u1[sel], u2[sel], model["dom"])
+            qe[sel] = 1.0
+            continue
+        if t["kind"] == "multipmt":
+            ids[sel], qe[sel] = _multipmt(pos[sel], dirs[sel], wl[sel], u1[sel], u2[sel],
+                                          np.asarray(t["position"], np.float32), radius,
+                                          model["multipmt"])
             continue
         m = model
         c0 = np.asarray(t["position"], np.float32)

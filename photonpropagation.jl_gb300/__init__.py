@@ -21,11 +21,16 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
 from .targets import Circular, HomogeneousDetector, Rectangular, Spherical
-from . import calc, particles, pom, surrogate, workloads
+from . import calc, detection, dom, generic_multipmt, particles, pom, surrogate, workloads
 from .particles import (Particle, cascade_cherenkov_track_length, particle_shape, propagate_particles,
                         rescale_source, split_source, total_lightyield)
 from .calc import (calc_tgeo, calc_tgeo_tracks, calc_time_residual, closest_approach_distance,
                    closest_approach_param)
-from .pom import POM, calc_pe_weight, make_hits_from_photons
+from .pom import POM
+from .dom import DOM, DOMAcceptance
+from .generic_multipmt import (SphericalMultiPMTTarget, fibonacci_sphere,
+                               make_generic_multipmt_om, make_generic_multipmt_positions)
+from .detection import (InterpQuantumEff, apply_qe, calc_pe_weight, check_pmt_hit_opening_angle,
+                        make_hits_from_photons)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -81,7 +81,11 @@ class pp_target(Structure):
 
 PP_PMT_HOMOGENEOUS = 0
 PP_PMT_POM = 1
+PP_PMT_DOM = 2
+PP_PMT_MULTIPMT = 3
 PP_POM_MAX_KNOTS = 128
+PP_DOM_MAX_POLY = 16
+PP_MULTIPMT_MAX_PMTS = 32
 
 
 class pp_pmt_target(Structure):
@@ -98,6 +102,28 @@ class pp_pom_model(Structure):
         ("qe", c_float * PP_POM_MAX_KNOTS), ("pmt_dir", (c_float * 3) * 16),
         ("pmt_group", c_int32 * 16),
     ]
+
+
+class pp_dom_model(Structure):
+    _fields_ = [
+        ("n_poly", c_int32), ("n_wl", c_int32), ("poly", c_float * PP_DOM_MAX_POLY),
+        ("polymax", c_float), ("zenith_axis", c_float * 3), ("apply_wl_acceptance", c_int32),
+        ("wl", c_float * PP_POM_MAX_KNOTS), ("wl_acc", c_float * PP_POM_MAX_KNOTS),
+    ]
+
+
+class pp_multipmt_model(Structure):
+    _fields_ = [
+        ("n_pmt", c_int32), ("n_qe", c_int32), ("pmt_area", c_float),
+        ("pmt_dir_module", (c_float * 3) * PP_MULTIPMT_MAX_PMTS),
+        ("pmt_dir", (c_float * 3) * PP_MULTIPMT_MAX_PMTS),
+        ("qe_wavelength", c_float * PP_POM_MAX_KNOTS), ("qe", c_float * PP_POM_MAX_KNOTS),
+    ]
+
+
+class pp_detection_models(Structure):
+    _fields_ = [("pom", POINTER(pp_pom_model)), ("dom", POINTER(pp_dom_model)),
+                ("multipmt", POINTER(pp_multipmt_model))]
 
 
 class pp_hit_record(Structure):
@@ -206,6 +232,9 @@ SIGNATURES = {
                               POINTER(c_double)]),
     "pp_make_hits_from_photons": (c_int32, [c_void_p, c_int64, POINTER(pp_pmt_target), c_int32,
                                             c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "pp_make_hits_from_photons_models": (c_int32, [c_void_p, c_int64, POINTER(pp_pmt_target),
+                                                   c_int32, POINTER(pp_detection_models), c_int64,
+                                                   c_void_p, c_void_p, c_void_p]),
     "pp_set_shaped_targets": (c_int32, [c_void_p, POINTER(pp_target), c_int32]),
     "pp_time_residuals": (c_int32, [c_void_p, c_int64, POINTER(c_double), c_int32, c_double,
                                     c_void_p, c_void_p]),

@@ -212,7 +212,7 @@ def propagate_particles(particles, targets, seed, medium, rng=None, device=0):
     propagation, time residuals, PMT hits and QE weights follow.  Returns
     the hit table, or None when no photon reached a module."""
     from .calc import calc_time_residual
-    from .pom import calc_pe_weight, make_hits_from_photons
+    from .detection import calc_pe_weight, make_hits_from_photons
     from .processing import propagate_photons
     from .propsetup import PhotonPropSetup
     spectrum = make_cherenkov_spectrum((300.0, 800.0), medium)

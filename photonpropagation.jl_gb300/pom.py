@@ -1,24 +1,14 @@
-"""Optical modules and the detection step after propagation.
+"""The 16-PMT P-ONE optical module (mirrors src/pom.jl).
 
-* ``POM``: the 16-PMT P-ONE optical module (src/pom.jl:63-112): a sphere of
-  radius 0.3 m, PMTs of 75 mm diameter, PMT directions from
-  ``make_pom_pmt_coordinates`` (src/pom.jl:114-142), the POMAcceptance tables
-  (assets/pmt_acc.hd5) and the relative quantum efficiency (assets/PMTAcc.csv),
-  both extracted into ``data/`` by ``data/extract_pom_tables.py``.
-* ``make_hits_from_photons`` / ``calc_pe_weight`` (src/processing.jl:88-205):
-  photon hits -> PMT hits, on the device (``pp_make_hits_from_photons``).
-
-Deliberate differences: the random numbers come from a Philox stream keyed on
-``seed`` and the hit's row (the reference uses Julia's global RNG); a
-homogeneous module is detected with probability active_area / (4 pi r^2) as
-PMT 1, the intent of check_pmt_hit(::HomogeneousTarget) (src/detection.jl:
-70-84), whose signature the reference's make_hits_from_photons cannot call;
-``calc_pe_weight`` applies the POM's relative QE table (the reference's
-apply_qe(::POM) reads a field the model does not have, src/pom.jl:307).
+``POM``: a sphere of radius 0.3 m, PMTs of 75 mm diameter, PMT directions from
+``make_pom_pmt_coordinates`` (src/pom.jl:114-142), the POMAcceptance tables
+(assets/pmt_acc.hd5) and the relative quantum efficiency (assets/PMTAcc.csv),
+both extracted into ``data/`` by ``data/extract_pom_tables.py``.  Detection
+(check_pmt_hit for a POM, src/pom.jl:246-305) runs on the device; detection.py
+drives it for every module kind.
 """
 from __future__ import annotations
 
-import ctypes
 import os
 from dataclasses import dataclass
 from typing import Sequence
@@ -26,8 +16,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import check
-from .targets import HomogeneousDetector, Spherical
+from .targets import Spherical
 
 _DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 POM_RADIUS = 0.3
@@ -134,99 +123,3 @@ def pom_model(orientation=None, tables: POMTables | None = None) -> "_lib.pp_pom
             m.pmt_dir[i][k] = float(d[i, k])
         m.pmt_group[i] = int(POM_PMT_GROUP[i])
     return m
-
-
-def pmt_targets(targets) -> "ctypes.Array":
-    """pp_pmt_target per propagation target (index i -> module_index i + 1)."""
-    arr = (_lib.pp_pmt_target * max(1, len(targets)))()
-    for i, t in enumerate(targets):
-        p = np.asarray(t.shape.position, np.float32).reshape(3)
-        arr[i].position[:] = (float(p[0]), float(p[1]), float(p[2]))
-        arr[i].radius = float(np.float32(t.shape.radius))
-        if isinstance(t, POM):
-            arr[i].kind = _lib.PP_PMT_POM
-            arr[i].active_area = float(t.pmt_area)
-        elif isinstance(t, HomogeneousDetector):
-            arr[i].kind = _lib.PP_PMT_HOMOGENEOUS
-            arr[i].active_area = float(t.pmt_area)
-        else:
-            raise TypeError(f"target {i}: no detection model for {type(t).__name__}")
-    return arr
-
-
-def make_hits_device(d_records: int, n: int, targets, seed: int, d_pmt_id: int,
-                     d_qe_weight: int = 0, orientation=None, stream: int = 0) -> None:
-    """Device form: hit records in device memory -> PMT ids (and QE weights)."""
-    lib = _lib.load()
-    tg = pmt_targets(targets)
-    pom = pom_model(orientation) if any(isinstance(t, POM) for t in targets) else None
-    check(lib.pp_make_hits_from_photons(ctypes.c_void_p(d_records), int(n), tg, len(targets),
-                                        ctypes.byref(pom) if pom is not None else None,
-                                        int(seed), ctypes.c_void_p(d_pmt_id),
-                                        ctypes.c_void_p(d_qe_weight or None),
-                                        ctypes.c_void_p(stream)), "pp_make_hits_from_photons")
-
-
-def records_from_table(table, targets) -> np.ndarray:
-    """pp_hit_record rows (positions, wavelengths, 1-based module index) of a
-    host hit table."""
-    n = table.nrow
-    rec = np.zeros(n, dtype=np.dtype(_lib.pp_hit_record))
-    rec["position"] = np.asarray(table["position"], np.float32).reshape(n, 3)
-    rec["wavelength"] = np.asarray(table["wavelength"], np.float32)
-    index_of = {int(getattr(t, "module_id", i + 1)): i + 1 for i, t in enumerate(targets)}
-    rec["module_index"] = np.array([index_of[int(m)] for m in table["module_id"]], np.int32) \
-        if n else np.zeros(0, np.int32)
-    return rec
-
-
-def _targets_of(setup_or_targets):
-    return getattr(setup_or_targets, "targets", setup_or_targets)
-
-
-def make_hits_from_photons(table, setup_or_targets, target_orientation=None,
-                           apply_wl_acc: bool = True, seed: int = 0, device: int = 0):
-    """``make_hits_from_photons(df, setup_or_targets, target_orientation)``
-    (src/processing.jl:88-139): the photons that a PMT detects, with a
-    ``pmt_id`` column (1-based).  The POM's wavelength acceptance is part of
-    its detection probability (its apply_wl_acceptance accepts all,
-    src/pom.jl:165-174), so ``apply_wl_acc`` changes nothing here."""
-    import torch
-    from .processing import HitTable
-    targets = _targets_of(setup_or_targets)
-    rec = records_from_table(table, targets)
-    n = len(rec)
-    out = HitTable()
-    if n == 0:
-        for k, v in table.items():
-            out[k] = v
-        out["pmt_id"] = np.zeros(0, np.int32)
-        return out
-    d_rec = torch.from_numpy(rec.view(np.uint8)).to(f"cuda:{device}")
-    d_id = torch.empty(n, dtype=torch.int32, device=f"cuda:{device}")
-    make_hits_device(d_rec.data_ptr(), n, targets, seed, d_id.data_ptr(),
-                     orientation=target_orientation)
-    ids = d_id.cpu().numpy()
-    mask = ids > 0
-    for k, v in table.items():
-        out[k] = np.asarray(v)[mask]
-    out["pmt_id"] = ids[mask]
-    return out
-
-
-def calc_pe_weight(table, setup_or_targets):
-    """``calc_pe_weight!(photons, targets)`` (src/processing.jl:179-205): a
-    ``qe_weight`` column (the POM's relative quantum efficiency at the
-    wavelength, 0 outside the table; 1 for homogeneous modules) multiplied
-    into ``total_weight``."""
-    targets = _targets_of(setup_or_targets)
-    t = load_pom_tables()
-    is_pom = {int(getattr(x, "module_id", i + 1)): isinstance(x, POM) for i, x in enumerate(targets)}
-    wl = np.asarray(table["wavelength"], np.float64)
-    qe = np.interp(wl, t.qe_wavelength, t.qe, left=0.0, right=0.0)
-    pom_rows = np.array([is_pom[int(m)] for m in table["module_id"]], bool) \
-        if len(wl) else np.zeros(0, bool)
-    qe = np.where(pom_rows, qe, 1.0)
-    table["qe_weight"] = qe
-    table["total_weight"] = np.asarray(table["total_weight"], np.float64) * qe
-    return table

@@ -64,7 +64,7 @@ def test_device_time_residuals(pp, gpu_ctx, track):
     table = pp.propagate_photons(s)
     assert table.nrow > 100
     pp.calc_time_residual(table, s)
-    rec = pp.pom.records_from_table(table, s.targets)
+    rec = pp.detection.records_from_table(table, s.targets)
     rec["time"] = table["time"]
     d_rec = torch.from_numpy(rec.view(np.uint8)).cuda()
     d_tres = torch.empty(table.nrow, dtype=torch.float64, device="cuda")

@@ -130,7 +130,7 @@ def test_device_detection_matches_oracle(pp, gpu_ctx, seed):
     d_rec = torch.from_numpy(rec.view(np.uint8)).cuda()
     d_id = torch.full((n,), -1, dtype=torch.int32, device="cuda")
     d_qe = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
-    pom.make_hits_device(d_rec.data_ptr(), n, targets, seed, d_id.data_ptr(), d_qe.data_ptr())
+    pp.detection.make_hits_device(d_rec.data_ptr(), n, targets, seed, d_id.data_ptr(), d_qe.data_ptr())
     got_id, got_qe = d_id.cpu().numpy(), d_qe.cpu().numpy()
     otargets = [dict(position=t.shape.position, radius=t.shape.radius,
                      kind="pom" if isinstance(t, pom.POM) else "homogeneous",
@@ -156,8 +156,8 @@ def test_make_hits_from_photons_end_to_end(pp, gpu_ctx):
                                                                                   medium), 3)
     table = pp.propagate_photons(setup)
     assert table.nrow > 5000
-    hits = pom.make_hits_from_photons(table, setup, seed=5)
-    again = pom.make_hits_from_photons(table, setup, seed=5)
+    hits = pp.detection.make_hits_from_photons(table, setup, seed=5)
+    again = pp.detection.make_hits_from_photons(table, setup, seed=5)
     np.testing.assert_array_equal(hits["pmt_id"], again["pmt_id"])
     m = _model_dict(pp)
     for t_ix, t in enumerate(targets):
@@ -171,6 +171,6 @@ def test_make_hits_from_photons_end_to_end(pp, gpu_ctx):
             got = (hits["pmt_id"][sel] == k + 1).sum()
             assert abs(got - exp) < 5 * np.sqrt(exp) + 5, (t_ix, k, got, exp)
     w0 = hits["total_weight"].copy()
-    pom.calc_pe_weight(hits, setup)
+    pp.detection.calc_pe_weight(hits, setup)
     qe = np.interp(hits["wavelength"], m["qe_wavelength"], m["qe"], left=0, right=0)
     np.testing.assert_allclose(hits["total_weight"], w0 * qe, rtol=1e-12)
