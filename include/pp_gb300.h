@@ -238,17 +238,28 @@ PP_API int pp_total_photons(const pp_ctx* ctx, int64_t* total);
  * horizontal (normal e_z) rectangle and disc of the reference's Rectangular
  * and Circular shapes.  With any non-spherical target the kernel tests every
  * target at every step in index order, as the reference does (no culling
- * grid); a list of spheres only takes the culled path of pp_set_targets. */
+ * grid); a list of spheres only takes the culled path of pp_set_targets.
+ *
+ * DetectorLines (the kernel variant of src/photon_prop_cuda.jl:552-694): the
+ * list is L groups of one PP_TARGET_LINE record (position[0..1] = the line's
+ * x, y; radius = its 2-D radius; reserved = N, the same for every line)
+ * followed by its N module records (any shape).  At each step the lines are
+ * tested in order with the 2-D ray-circle test of the step's (x, y) start
+ * and its unnormalised (x, y) direction over the 3-D step length; the first
+ * crossed line ends the search whether or not one of its modules is hit, and
+ * a hit on module t (1-based) of line l (1-based) reports module index
+ * t + N * l, all as the reference computes them.  N * (L + 1) <= 65535. */
 #define PP_TARGET_SPHERE 0
 #define PP_TARGET_RECTANGLE 1
 #define PP_TARGET_DISC 2
+#define PP_TARGET_LINE 3
 typedef struct pp_target {
   float position[3];
-  float radius;      /* sphere, disc */
+  float radius;      /* sphere, disc, line */
   float length_x;    /* rectangle */
   float length_y;    /* rectangle */
   int32_t kind;      /* PP_TARGET_* */
-  int32_t reserved;
+  int32_t reserved;  /* line: modules per line */
 } pp_target;
 PP_API int pp_set_shaped_targets(pp_ctx* ctx, const pp_target* t, int32_t n);
 

@@ -190,7 +190,7 @@ class Run:
         shaped = setup.has_shaped_targets()
         return cls(setup.source_records(), len(setup.sources),
                    None if shaped else setup.sphere_records(),
-                   len(setup.targets), setup.medium.oracle_params(),
+                   setup.n_target_records(), setup.medium.oracle_params(),
                    shape_records=setup.target_records() if shaped else None,
                    spectrum_knots=setup.spectrum_knots,
                    mono_wavelength=setup.mono_wavelength or 0.0,

@@ -20,7 +20,8 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
                       PointlikeIsotropicEmitter, PointlikeTimeRangeEmitter, source_photons)
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
                        make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
-from .targets import Circular, HomogeneousDetector, Rectangular, Spherical
+from .targets import (Circular, DetectorLine, DetectorLines, HomogeneousDetector, Rectangular,
+                      Spherical)
 from . import calc, detection, dom, generic_multipmt, particles, pom, surrogate, workloads
 from .particles import (Particle, cascade_cherenkov_track_length, particle_shape, propagate_particles,
                         rescale_source, split_source, total_lightyield)

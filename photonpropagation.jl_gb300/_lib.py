@@ -72,6 +72,7 @@ class pp_tuning(Structure):
 PP_TARGET_SPHERE = 0
 PP_TARGET_RECTANGLE = 1
 PP_TARGET_DISC = 2
+PP_TARGET_LINE = 3
 
 
 class pp_target(Structure):

@@ -533,13 +533,33 @@ PP_API int pp_set_shaped_targets(pp_ctx* ctx, const pp_target* t, int32_t n) {
   wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || n < 0 || (n > 0 && !t)) return set_error(PP_ERR_INVALID, "bad target list");
   if (n > 65535) return set_error(PP_ERR_INVALID, "at most 65535 targets are supported");
-  bool spheres_only = true;
+  // DetectorLines: groups of one line record and its N modules
+  const bool lines = n > 0 && t[0].kind == PP_TARGET_LINE;
+  const int per_line = lines ? t[0].reserved : 0;
+  if (lines) {
+    if (per_line < 1 || n % (per_line + 1) != 0)
+      return set_error(PP_ERR_INVALID, "detector lines: %d records are not groups of 1 + %d", n,
+                       per_line);
+    const long long n_lines = n / (per_line + 1);
+    if ((long long)per_line * (n_lines + 1) > 65535)
+      return set_error(PP_ERR_INVALID, "detector lines: module index N * (L + 1) exceeds 65535");
+  }
+  bool spheres_only = !lines;
   for (int i = 0; i < n; ++i) {
     const pp_target& x = t[i];
     if (!std::isfinite(x.position[0]) || !std::isfinite(x.position[1]) ||
         !std::isfinite(x.position[2]))
       return set_error(PP_ERR_INVALID, "target %d has a non-finite position", i);
-    if (x.kind == PP_TARGET_SPHERE || x.kind == PP_TARGET_DISC) {
+    const bool line_slot = lines && i % (per_line + 1) == 0;
+    if (line_slot != (x.kind == PP_TARGET_LINE))
+      return set_error(PP_ERR_INVALID, "target %d: line records must head each group of %d modules",
+                       i, per_line);
+    if (x.kind == PP_TARGET_LINE) {
+      if (x.reserved != per_line)
+        return set_error(PP_ERR_INVALID, "target %d: every line must hold %d modules", i, per_line);
+      if (!(x.radius > 0.0f) || !std::isfinite(x.radius))
+        return set_error(PP_ERR_INVALID, "target %d: line radius must be > 0", i);
+    } else if (x.kind == PP_TARGET_SPHERE || x.kind == PP_TARGET_DISC) {
       if (!(x.radius > 0.0f) || !std::isfinite(x.radius))
         return set_error(PP_ERR_INVALID, "target %d: radius must be > 0", i);
     } else if (x.kind == PP_TARGET_RECTANGLE) {
@@ -567,12 +587,14 @@ PP_API int pp_set_shaped_targets(pp_ctx* ctx, const pp_target* t, int32_t n) {
   for (int i = 0; i < n; ++i) {
     const pp_target& x = t[i];
     const bool rect = x.kind == PP_TARGET_RECTANGLE;
+    const bool line = x.kind == PP_TARGET_LINE;
     const float p0 = rect ? 0.5f * x.length_x : x.radius * x.radius;
-    const float p1 = rect ? 0.5f * x.length_y : 0.0f;
+    float p1 = rect ? 0.5f * x.length_y : 0.0f;
+    if (line) memcpy(&p1, &x.reserved, sizeof(p1));  // modules that follow
     int kind = x.kind;
     float kf;
     memcpy(&kf, &kind, sizeof(kf));
-    h[2 * i] = make_float4(x.position[0], x.position[1], x.position[2], p0);
+    h[2 * i] = make_float4(x.position[0], x.position[1], line ? 0.0f : x.position[2], p0);
     h[2 * i + 1] = make_float4(p1, kf, 0.0f, 0.0f);
   }
   PP_CUDA(cudaMalloc(&ctx->d_shapes, sizeof(float4) * h.size()), "cudaMalloc(shaped targets)");

@@ -214,7 +214,8 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
 #endif
 
 // kShapes: shaped targets (a.shapes), every target tested at every step in
-// index order (no grid, no deferred queue).
+// index order (no grid, no deferred queue); a list of detector lines is
+// searched line by line (src/photon_prop_cuda.jl:611-634).
 template <bool kPrecise, bool kSmemGrid, bool kShapes = false>
 __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
     propagate_kernel(const __grid_constant__ LaunchArgs a) {
@@ -367,20 +368,45 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         const float step = -f_log<kPrecise>(u01(r.x)) * sca_len;
         if constexpr (kShapes) {
           if (active && !found) {
+            int hit = -1;  // 0-based module index to report
+            float d = 0.0f;
+            int line_no = 0;
             for (int j = 0; j < a.n_shapes; ++j) {
-              float d;
-              if (shape_hit<kPrecise>(a.shapes, j, pos, dir, step, &d)) {
-                found = true;
-                best.key[lane] = ((uint32_t)k << 16) | (uint32_t)j;
-                best.hx[lane] = madd<kPrecise>(dir.x, d, pos.x);
-                best.hy[lane] = madd<kPrecise>(dir.y, d, pos.y);
-                best.hz[lane] = madd<kPrecise>(dir.z, d, pos.z);
-                best.ox[lane] = dir.x;
-                best.oy[lane] = dir.y;
-                best.oz[lane] = dir.z;
-                best.dist[lane] = (dist - comp) + d;
+              const float4 h = __ldg(a.shapes + 2 * j + 1);
+              if (__float_as_int(h.y) == PP_TARGET_LINE) {
+                // DetectorLines: the 2-D test of the line, then its modules;
+                // the first crossed line ends the search
+                const int nm = __float_as_int(h.x);
+                ++line_no;
+                float dl;
+                if (!sphere_hit<kPrecise>(__ldg(a.shapes + 2 * j), make_float3(pos.x, pos.y, 0.0f),
+                                          make_float3(dir.x, dir.y, 0.0f), step, &dl)) {
+                  j += nm;
+                  continue;
+                }
+                for (int m = 1; m <= nm; ++m) {
+                  if (shape_hit<kPrecise>(a.shapes, j + m, pos, dir, step, &d)) {
+                    hit = m + nm * line_no - 1;
+                    break;
+                  }
+                }
                 break;
               }
+              if (shape_hit<kPrecise>(a.shapes, j, pos, dir, step, &d)) {
+                hit = j;
+                break;
+              }
+            }
+            if (hit >= 0) {
+              found = true;
+              best.key[lane] = ((uint32_t)k << 16) | (uint32_t)hit;
+              best.hx[lane] = madd<kPrecise>(dir.x, d, pos.x);
+              best.hy[lane] = madd<kPrecise>(dir.y, d, pos.y);
+              best.hz[lane] = madd<kPrecise>(dir.z, d, pos.z);
+              best.ox[lane] = dir.x;
+              best.oy[lane] = dir.y;
+              best.oz[lane] = dir.z;
+              best.dist[lane] = (dist - comp) + d;
             }
           }
         } else {

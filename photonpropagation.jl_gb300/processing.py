@@ -7,6 +7,7 @@ import numpy as np
 from . import _lib
 from .context import Context, device_memory
 from .sources import to_records
+from . import targets as _targets
 from .targets import module_ids
 
 _CONTEXTS: dict = {}
@@ -54,7 +55,7 @@ def get_context(device: int = 0) -> Context:
 
 
 def _ensure_uploaded(setup, ctx) -> None:
-    key = (id(ctx), id(setup.medium), id(setup.spec_dist), tuple(id(t) for t in setup.targets),
+    key = (id(ctx), id(setup.medium), id(setup.spec_dist), _targets.identity(setup.targets),
            setup.needs_track_smear())
     if getattr(setup, "_uploaded_key", None) != key:
         setup.upload(ctx)
@@ -116,6 +117,7 @@ def propagate_photons(setup, *buffers, steps: int = 15, reserved_memory_fraction
             rest.pop(0)
     if rest:
         steps = int(rest.pop(0))
+    ids = module_ids(setup.targets)  # raises for DetectorLines, as the reference does
     if hb is None:
         hb = make_hit_buffers(reserved_memory_fraction=reserved_memory_fraction, device=device)
     cols, n_ph_sim = _run(setup, hb, steps)
@@ -124,7 +126,6 @@ def propagate_photons(setup, *buffers, steps: int = 15, reserved_memory_fraction
     for k in ("position", "direction", "initial_direction", "wavelength", "time",
               "dist_travelled"):
         t[k] = cols[k]
-    ids = module_ids(setup.targets)
     t["module_id"] = ids[cols["module_index"] - 1] if n else np.zeros(0, np.uint16)
     t["n_steps"] = cols["n_steps"]
     total = sum(int(s.photons) for s in setup.sources)

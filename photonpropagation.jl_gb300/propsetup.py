@@ -26,7 +26,7 @@ class PhotonPropSetup:
     def __init__(self, sources, targets, medium, spectrum, seed, photon_scaling=1.0,
                  spectrum_interp_steps=600, track_smear=None):
         self.sources = list(sources)
-        self.targets = list(targets)
+        self.targets = targets if isinstance(targets, _targets.DetectorLines) else list(targets)
         self.medium = medium
         if isinstance(spectrum, Spectrum):
             dist = spectrum.spectral_dist
@@ -78,6 +78,9 @@ class PhotonPropSetup:
     def target_records(self):
         return _targets.to_targets(self.targets)
 
+    def n_target_records(self) -> int:
+        return _targets.record_count(self.targets)
+
     def upload(self, ctx, cell_size: float = 0.0) -> None:
         """Send medium, spectrum, track table and targets to a Context."""
         ctx.set_medium(self.medium_tables())
@@ -88,6 +91,6 @@ class PhotonPropSetup:
         if self.needs_track_smear():
             ctx.set_track_smear(self.track_quantiles())
         if self.has_shaped_targets():
-            ctx.set_shaped_targets(self.target_records(), len(self.targets))
+            ctx.set_shaped_targets(self.target_records(), self.n_target_records())
         else:
             ctx.set_targets(self.sphere_records(), len(self.targets), cell_size)

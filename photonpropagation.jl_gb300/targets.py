@@ -41,6 +41,51 @@ class HomogeneousDetector:
     module_id: int
 
 
+@dataclass
+class DetectorLine:
+    """DetectorLine(x_pos, y_pos, radius, targets) (src/photon_prop_cuda.jl:418-423):
+    a vertical line at (x_pos, y_pos) whose module shapes lie within `radius`
+    of it in the xy plane."""
+    x_pos: float
+    y_pos: float
+    radius: float
+    targets: Sequence
+
+
+@dataclass
+class DetectorLines:
+    """DetectorLines(lines) (src/photon_prop_cuda.jl:425-427): lines with the
+    same number of modules each, searched line by line in the kernel.  Not
+    iterable, as in the reference."""
+    lines: Sequence[DetectorLine]
+
+    def __post_init__(self):
+        self.lines = list(self.lines)
+        if not self.lines:
+            raise ValueError("DetectorLines needs at least one line")
+        n = len(self.lines[0].targets)
+        if n < 1 or any(len(line.targets) != n for line in self.lines):
+            raise ValueError("every DetectorLine must hold the same number (>= 1) of modules")
+
+    @property
+    def modules_per_line(self) -> int:
+        return len(self.lines[0].targets)
+
+
+def record_count(targets) -> int:
+    """Number of pp_target records for `targets` (a line adds one record)."""
+    if isinstance(targets, DetectorLines):
+        return len(targets.lines) * (targets.modules_per_line + 1)
+    return len(targets)
+
+
+def identity(targets) -> tuple:
+    """Key of a target list for upload caching."""
+    if isinstance(targets, DetectorLines):
+        return (id(targets),) + tuple(id(t) for line in targets.lines for t in line.targets)
+    return tuple(id(t) for t in targets)
+
+
 def to_spheres(targets) -> "_lib.pp_sphere array":
     arr = (_lib.pp_sphere * max(1, len(targets)))()
     for i, t in enumerate(targets):
@@ -54,13 +99,30 @@ def to_spheres(targets) -> "_lib.pp_sphere array":
 
 
 def is_shaped(targets) -> bool:
-    """True when a target is not a sphere (then every target is tested at
-    every step, with no culling grid)."""
+    """True when a target is not a sphere or the targets are detector lines
+    (then the targets are tested at every step in order, with no culling
+    grid)."""
+    if isinstance(targets, DetectorLines):
+        return True
     return any(not isinstance(getattr(t, "shape", t), Spherical) for t in targets)
 
 
 def to_targets(targets) -> "_lib.pp_target array":
-    """pp_target records (any shape) in index order."""
+    """pp_target records (any shape) in index order; detector lines as one
+    PP_TARGET_LINE record followed by the line's modules, line by line."""
+    if isinstance(targets, DetectorLines):
+        n = targets.modules_per_line
+        arr = (_lib.pp_target * record_count(targets))()
+        for li, line in enumerate(targets.lines):
+            head = arr[li * (n + 1)]
+            head.position[:] = (float(np.float32(line.x_pos)), float(np.float32(line.y_pos)), 0.0)
+            head.radius = float(np.float32(line.radius))
+            head.kind = _lib.PP_TARGET_LINE
+            head.reserved = n
+            mods = to_targets(list(line.targets))
+            for m in range(n):
+                arr[li * (n + 1) + 1 + m] = mods[m]
+        return arr
     arr = (_lib.pp_target * max(1, len(targets)))()
     for i, t in enumerate(targets):
         shape = getattr(t, "shape", t)
@@ -83,5 +145,10 @@ def to_targets(targets) -> "_lib.pp_target array":
 
 def module_ids(targets) -> np.ndarray:
     """module_id of each target (index i -> id), as UInt16 in the reference."""
+    if isinstance(targets, DetectorLines):
+        # src/processing.jl:67 iterates setup.targets, which DetectorLines does not support
+        raise TypeError("DetectorLines has no module ids to map: propagate_photons fails on it "
+                        "as in the reference; run_photon_prop_no_local_cache returns the "
+                        "kernel's module index t + N * line")
     return np.asarray([int(getattr(t, "module_id", i + 1)) for i, t in enumerate(targets)],
                       np.uint16)
