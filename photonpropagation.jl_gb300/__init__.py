@@ -10,8 +10,9 @@ from . import _lib
 from .context import Context, debug_philox, device_memory, measure_fp32_peak
 from .medium import (C_VAC_M_NS, CascadiaMediumProperties, MediumProperties,
                      SimpleMediumProperties)
-from .processing import (HitBuffers, HitTable, PhotonPropOOMException, calc_total_weight,
-                         get_context, make_hit_buffers, propagate_photons,
+from .processing import (HitBuffers, HitTable, PhotonPropOOMException, add_pmt_noise,
+                         calc_number_of_steps, calc_total_weight, get_context, get_pmt_count,
+                         make_hit_buffers, propagate_photons, resample_hits,
                          run_photon_prop_no_local_cache)
 from .propsetup import PhotonPropSetup
 from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropicEmitter,

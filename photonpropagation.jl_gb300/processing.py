@@ -137,3 +137,75 @@ def propagate_photons(setup, *buffers, steps: int = 15, reserved_memory_fraction
     t["source_index"] = cols["source_index"]
     t.n_ph_sim = n_ph_sim
     return t
+
+
+def calc_number_of_steps(sca_len: float, cutoff_distance: float, percentile: float = 0.9) -> int:
+    """``calc_number_of_steps`` (src/processing.jl:154-177): the smallest n from
+    ceil(cutoff / sca_len) up such that a fraction `percentile` of photons has
+    travelled further than `cutoff_distance` after n steps, the path after n
+    exponential steps being Erlang(n, sca_len)."""
+    from scipy import stats
+    n = int(np.ceil(cutoff_distance / sca_len))
+    while stats.gamma.ppf(1.0 - percentile, n, scale=sca_len) <= cutoff_distance:
+        n += 1
+    return n
+
+
+def resample_hits(hits: HitTable, replace: bool = False, rng=None) -> HitTable:
+    """``resample_hits(hits, replace=false)`` (src/processing.jl:141-152): for
+    each (module_id, pmt_id) a Poisson number of hits with mean the sum of
+    their total_weight, drawn from them with probabilities proportional to
+    the weights (without replacement unless `replace`)."""
+    rng = rng if rng is not None else np.random.default_rng()
+    mid = np.asarray(hits["module_id"]).astype(np.int64)
+    pid = np.asarray(hits["pmt_id"]).astype(np.int64)
+    w = np.asarray(hits["total_weight"], np.float64)
+    keys = np.stack([mid, pid], axis=1)
+    groups, inverse = np.unique(keys, axis=0, return_inverse=True)
+    rows = []
+    for g in range(len(groups)):
+        idx = np.flatnonzero(inverse.reshape(-1) == g)
+        wsum = w[idx].sum()
+        k = int(rng.poisson(wsum))
+        if k > len(idx) and not replace:
+            raise ValueError(f"cannot draw {k} hits without replacement from {len(idx)}")
+        rows.append(rng.choice(idx, size=k, replace=replace, p=w[idx] / wsum))
+    take = np.concatenate(rows) if rows else np.zeros(0, np.int64)
+    out = HitTable()
+    for key, v in hits.items():
+        out[key] = np.asarray(v)[take]
+    return out
+
+
+def get_pmt_count(target) -> int:
+    """PMTs of a module: 16 for a POM, 1 for a DOM or a homogeneous module, the
+    layout's count for a multi-PMT module."""
+    from .generic_multipmt import SphericalMultiPMTTarget
+    from .generic_multipmt import get_pmt_count as multipmt_count
+    from .pom import POM
+    if isinstance(target, POM):
+        return 16
+    if isinstance(target, SphericalMultiPMTTarget):
+        return multipmt_count(target)
+    return 1
+
+
+def add_pmt_noise(hits: list, targets, noise_rate: float = 1e4, time_window: float = 1e4,
+                  rng=None, n_pmt: int | None = None) -> list:
+    """``add_pmt_noise!(hits, targets; noise_rate=1E4, time_window=1E4)``
+    (src/processing.jl:246-265): `hits` holds one array of hit times (ns) per
+    (PMT, target), PMT fastest, n_pmt = get_pmt_count(first(targets)); each
+    gets a Poisson number (mean noise_rate [Hz] * time_window [ns] * 1e-9) of
+    times uniform on [-time_window / 2, time_window / 2], then is sorted.
+    Returns `hits`."""
+    rng = rng if rng is not None else np.random.default_rng()
+    n_pmt = get_pmt_count(targets[0]) if n_pmt is None else int(n_pmt)
+    mean = noise_rate * 1e-9 * time_window
+    for tix in range(len(targets)):
+        for pmt in range(n_pmt):
+            i = pmt + n_pmt * tix
+            k = int(rng.poisson(mean))
+            if k > 0:
+                noise = rng.uniform(-time_window / 2, time_window / 2, k)
+                hits[i] = np.sort(np.concatenate([np.asarray(hits[i], np.float64), noise]))
+    return hits
