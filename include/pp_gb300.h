@@ -78,7 +78,7 @@ extern "C" {
  * split into photon ranges (shards, replays) with identical results. */
 typedef struct pp_source {
   int32_t kind;           /* PP_SRC_*                                         */
-  int32_t reserved0;
+  int32_t smear_table;    /* Cherenkov kinds: track-smear table (0 = first)   */
   int64_t photons;        /* PhotonSource.photons (Int64)                     */
   float position[3];      /* m                                                */
   float time;             /* ns; time_range[1] for POINTLIKE_TIME_RANGE       */
@@ -216,6 +216,14 @@ PP_API int pp_set_monochromatic(pp_ctx* ctx, float wavelength_nm);
  * called at src/photon_prop_cuda.jl:89).  Needed by Cherenkov emitters. */
 PP_API int pp_set_track_smear(pp_ctx* ctx, const float* cos_theta_quantiles, int32_t n);
 
+/* n_tables such tables of n knots each, table t at cos_theta_quantiles[t * n];
+ * a Cherenkov source draws from table pp_source.smear_table.  One table per
+ * distinct Beta(a, b) of ExtendedCherenkovEmitterCustomSmear (track cos theta
+ * = 2 Beta(a, b) - 1, src/photon_prop_cuda.jl:134-154, src/lightyield.jl:
+ * 725-769).  pp_set_track_smear is the one-table form. */
+PP_API int pp_set_track_smear_tables(pp_ctx* ctx, const float* cos_theta_quantiles, int32_t n,
+                                     int32_t n_tables);
+
 /* Upload spherical targets and build the uniform culling grid on the device.
  * cell_size <= 0 picks a size automatically.  Replaces CuVector(targets)
  * (src/photon_prop_cuda.jl:910-912). */
@@ -324,7 +332,8 @@ PP_API int pp_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_
  * while another framework's pooling allocator owns the device memory, code
  * recorded into a CUDA graph by its caller, services that fix their memory
  * use at start-up.  Inputs are host arrays (medium tables, spectrum knots or
- * a monochromatic wavelength, track table, targets, sources); hits go to the
+ * a monochromatic wavelength, one track table (sources' smear_table 0),
+ * spherical targets, sources); hits go to the
  * caller's device buffer d_hits (16-byte aligned, `capacity` records) and the
  * launch's counters to the host struct *counters.  All scratch (device copies
  * of the inputs, culling grid, safety field, work queue, counters) comes from

@@ -181,7 +181,7 @@ class Run:
             tq = np.ascontiguousarray(track_quantiles, np.float32)
             self._keep.append(tq)
             r.track_quantiles = tq.ctypes.data_as(POINTER(c_float))
-            r.n_track = tq.shape[0]
+            r.n_track = tq.shape[-1]  # knots per table (tables stacked row-wise)
         r.seed = seed
         self.run = r
 
@@ -194,7 +194,7 @@ class Run:
                    shape_records=setup.target_records() if shaped else None,
                    spectrum_knots=setup.spectrum_knots,
                    mono_wavelength=setup.mono_wavelength or 0.0,
-                   track_quantiles=setup.track_quantiles() if setup.needs_track_smear() else None,
+                   track_quantiles=setup.track_table_stack() if setup.needs_track_smear() else None,
                    seed=setup.seed, n_steps=n_steps, photon_scaling=setup.photon_scaling)
 
     def source_photons(self, src: int) -> int:

@@ -16,7 +16,8 @@ from .processing import (HitBuffers, HitTable, PhotonPropOOMException, add_pmt_n
                          run_photon_prop_no_local_cache)
 from .propsetup import PhotonPropSetup
 from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropicEmitter,
-                      ExtendedCherenkovEmitter, ExtendedCherenkovEmitterNoSmear,
+                      ExtendedCherenkovEmitter, ExtendedCherenkovEmitterCustomSmear,
+                      ExtendedCherenkovEmitterNoSmear,
                       LongitudinalParameterisation, PencilEmitter, PointlikeCherenkovEmitter,
                       PointlikeIsotropicEmitter, PointlikeTimeRangeEmitter, source_photons)
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,

@@ -39,7 +39,7 @@ PP_SRC_AXICONE = 8
 
 class pp_source(Structure):
     _fields_ = [
-        ("kind", c_int32), ("reserved0", c_int32), ("photons", c_int64),
+        ("kind", c_int32), ("smear_table", c_int32), ("photons", c_int64),
         ("position", c_float * 3), ("time", c_float),
         ("direction", c_float * 3), ("time_end", c_float),
         ("long_a", c_float), ("long_b", c_float), ("long_lrad", c_float), ("length", c_float),
@@ -186,6 +186,7 @@ SIGNATURES = {
     "pp_set_spectrum": (c_int32, [c_void_p, POINTER(c_float), c_int32]),
     "pp_set_monochromatic": (c_int32, [c_void_p, c_float]),
     "pp_set_track_smear": (c_int32, [c_void_p, POINTER(c_float), c_int32]),
+    "pp_set_track_smear_tables": (c_int32, [c_void_p, POINTER(c_float), c_int32, c_int32]),
     "pp_set_targets": (c_int32, [c_void_p, POINTER(pp_sphere), c_int32, c_float]),
     "pp_set_sources": (c_int32, [c_void_p, POINTER(pp_source), c_int32, c_float]),
     "pp_set_tuning": (c_int32, [c_void_p, POINTER(pp_tuning)]),

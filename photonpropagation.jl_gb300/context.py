@@ -126,6 +126,13 @@ class Context:
         check(self._lib.pp_set_track_smear(self.ptr, q.ctypes.data_as(ctypes.POINTER(c_float)),
                                            q.shape[0]), "pp_set_track_smear")
 
+    def set_track_smear_tables(self, q) -> None:
+        """(n_tables, n_knots) quantile tables; a source uses its smear_table."""
+        q = np.ascontiguousarray(np.atleast_2d(q), np.float32)
+        check(self._lib.pp_set_track_smear_tables(
+            self.ptr, q.ctypes.data_as(ctypes.POINTER(c_float)), q.shape[1], q.shape[0]),
+            "pp_set_track_smear_tables")
+
     def set_targets(self, spheres, n: int, cell_size: float = 0.0) -> None:
         check(self._lib.pp_set_targets(self.ptr, spheres, n, float(cell_size)), "pp_set_targets")
 

@@ -123,9 +123,11 @@ struct pp_ctx {
   float mono = 0.0f;
   bool has_spectrum = false;
 
-  // Cherenkov track smear quantiles
+  // Cherenkov track smear quantiles: n_track_tables tables of n_track knots
   float* d_track = nullptr;
   int n_track = 0;
+  int n_track_tables = 0;
+  int max_smear_table = 0;  // largest smear_table of the track-using sources
 
   // targets and grid
   std::vector<pp_sphere> h_targets;
@@ -251,6 +253,9 @@ int check_ready(const pp_ctx* ctx) {
   if (ctx->needs_track && ctx->n_track < 2)
     return set_error(PP_ERR_NOT_READY,
                      "Cherenkov emitters need the track-direction table (pp_set_track_smear)");
+  if (ctx->needs_track && ctx->max_smear_table >= ctx->n_track_tables)
+    return set_error(PP_ERR_NOT_READY, "a source uses track-smear table %d of %d uploaded",
+                     ctx->max_smear_table, ctx->n_track_tables);
   return PP_OK;
 }
 
@@ -482,20 +487,31 @@ PP_API int pp_set_monochromatic(pp_ctx* ctx, float wavelength) {
   return PP_OK;
 }
 
-PP_API int pp_set_track_smear(pp_ctx* ctx, const float* q, int32_t n) {
+PP_API int pp_set_track_smear_tables(pp_ctx* ctx, const float* q, int32_t n, int32_t n_tables) {
   wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !q || n < 2) return set_error(PP_ERR_INVALID, "track table needs n >= 2 knots");
-  for (int i = 0; i < n; ++i)
+  if (n_tables < 1 || (long long)n * n_tables > (1ll << 26))
+    return set_error(PP_ERR_INVALID, "track tables: need 1 <= n_tables and n * n_tables <= 2^26");
+  const long long total = (long long)n * n_tables;
+  for (long long i = 0; i < total; ++i)
     if (!(q[i] >= -1.0f && q[i] <= 1.0f))
-      return set_error(PP_ERR_INVALID, "track quantile %d outside [-1, 1]", i);
+      return set_error(PP_ERR_INVALID, "track quantile %lld outside [-1, 1]", i);
   DeviceScope ds(ctx->device);
   cudaFree(ctx->d_track);
   ctx->d_track = nullptr;
-  PP_CUDA(cudaMalloc(&ctx->d_track, sizeof(float) * n), "cudaMalloc(track)");
-  PP_CUDA(cudaMemcpy(ctx->d_track, q, sizeof(float) * n, cudaMemcpyHostToDevice), "upload track");
+  ctx->n_track = 0;
+  ctx->n_track_tables = 0;
+  PP_CUDA(cudaMalloc(&ctx->d_track, sizeof(float) * total), "cudaMalloc(track)");
+  PP_CUDA(cudaMemcpy(ctx->d_track, q, sizeof(float) * total, cudaMemcpyHostToDevice),
+          "upload track");
   ctx->n_track = n;
+  ctx->n_track_tables = n_tables;
   ctx->version++;
   return PP_OK;
+}
+
+PP_API int pp_set_track_smear(pp_ctx* ctx, const float* q, int32_t n) {
+  return pp_set_track_smear_tables(ctx, q, n, 1);
 }
 
 PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell_size) {
@@ -611,6 +627,7 @@ PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float phot
   if (!(photon_scaling >= 0.0f) || !std::isfinite(photon_scaling))
     return set_error(PP_ERR_INVALID, "photon_scaling must be finite and >= 0");
   bool needs_track = false;
+  int max_table = 0;
   for (int i = 0; i < n; ++i) {
     const pp_source& x = s[i];
     if (x.kind < 0 || x.kind >= PP_SRC_KIND_COUNT)
@@ -620,12 +637,18 @@ PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float phot
       if (!(x.long_a > 0.0f) || !(x.long_b > 0.0f) || !(x.long_lrad >= 0.0f))
         return set_error(PP_ERR_INVALID, "source %d: longitudinal parameters must be positive", i);
     }
-    if (kind_uses_track(x.kind)) needs_track = true;
+    if (kind_uses_track(x.kind)) {
+      if (x.smear_table < 0)
+        return set_error(PP_ERR_INVALID, "source %d: negative track-smear table", i);
+      needs_track = true;
+      max_table = std::max(max_table, (int)x.smear_table);
+    }
   }
   DeviceScope ds(ctx->device);
   ctx->h_sources.assign(s, s + n);
   ctx->scaling = photon_scaling;
   ctx->needs_track = needs_track;
+  ctx->max_smear_table = max_table;
   int rc = build_queue(ctx);
   ctx->has_sources = rc == PP_OK;
   return rc;

@@ -346,9 +346,9 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
                               spos.z + along * saxis.z);
             t0 = stime + along / kCVac;
           }
-          dir = cherenkov_dir<kPrecise>(saxis, med.w, u1, u2, u3,
-                                        kind != PP_SRC_EXTENDED_CHERENKOV_NOSMEAR, a.track,
-                                        a.n_track);
+          dir = cherenkov_dir<kPrecise>(
+              saxis, med.w, u1, u2, u3, kind != PP_SRC_EXTENDED_CHERENKOV_NOSMEAR,
+              a.track + (size_t)__ldg(&sp->smear_table) * (size_t)a.n_track, a.n_track);
           break;
         }
         default:

@@ -209,8 +209,11 @@ extern "C" PP_API int pp_propagate_static(
     if ((k == PP_SRC_EXTENDED_CHERENKOV || k == PP_SRC_EXTENDED_CHERENKOV_NOSMEAR) &&
         !(sources[i].long_a > 0.0f && sources[i].long_b > 0.0f))
       return fail(PP_ERR_INVALID, "source " + std::to_string(i) + ": bad longitudinal parameters");
-    needs_track |= k == PP_SRC_EXTENDED_CHERENKOV || k == PP_SRC_POINTLIKE_CHERENKOV ||
-                   k == PP_SRC_CHERENKOV_TRACK;
+    const bool track = k == PP_SRC_EXTENDED_CHERENKOV || k == PP_SRC_POINTLIKE_CHERENKOV ||
+                       k == PP_SRC_CHERENKOV_TRACK;
+    if (track && sources[i].smear_table != 0)  // one table here
+      return fail(PP_ERR_INVALID, "source " + std::to_string(i) + ": smear_table must be 0");
+    needs_track |= track;
   }
   if (needs_track && (n_track < 2 || !track_quantiles))
     return fail(PP_ERR_INVALID, "Cherenkov emitters need the track-direction table");

@@ -158,6 +158,18 @@ def extended_cherenkov_emitter(particle, medium, spectrum, oversample=1.0, rng=N
     return cls(list(particle.position), list(particle.direction), particle.time, n, lp)
 
 
+def extended_cherenkov_emitter_custom_smear(particle, medium, spectrum, cherenkov_beta_a=1.776,
+                                            cherenkov_beta_b=0.164, oversample=1.0, rng=None):
+    """ExtendedCherenkovEmitterCustomSmear(particle, medium, spectrum;
+    cherenkov_beta_a, cherenkov_beta_b, oversample) (src/lightyield.jl:756-769)."""
+    from .sources import ExtendedCherenkovEmitterCustomSmear
+    lp = LongitudinalParameterisation.from_energy(particle.energy, medium, particle.type)
+    n = _poisson(total_lightyield(particle, medium, spectrum) * oversample, rng)
+    return ExtendedCherenkovEmitterCustomSmear(list(particle.position), list(particle.direction),
+                                               particle.time, n, lp, float(cherenkov_beta_a),
+                                               float(cherenkov_beta_b))
+
+
 def pointlike_cherenkov_emitter(particle, medium, spectrum, rng=None):
     """PointlikeCherenkovEmitter(particle, medium, spectrum) (src/lightyield.jl:765-775)."""
     n = _poisson(total_lightyield(particle, medium, spectrum), rng)

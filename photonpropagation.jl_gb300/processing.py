@@ -6,7 +6,6 @@ import numpy as np
 
 from . import _lib
 from .context import Context, device_memory
-from .sources import to_records
 from . import targets as _targets
 from .targets import module_ids
 
@@ -65,7 +64,7 @@ def _ensure_uploaded(setup, ctx) -> None:
 def _run(setup, hit_buffers: HitBuffers, n_steps: int):
     ctx = get_context(hit_buffers.device)
     _ensure_uploaded(setup, ctx)
-    recs = to_records(setup.sources)
+    recs = setup.source_records()
     rc, n_hits, n_ph_sim = ctx.propagate(recs, len(setup.sources), setup.seed, n_steps,
                                          setup.photon_scaling, hit_buffers.capacity)
     if rc == _lib.PP_ERR_OVERFLOW:

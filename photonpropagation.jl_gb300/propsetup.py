@@ -66,8 +66,40 @@ class PhotonPropSetup:
             self._track = beta_track_quantiles()
         return self._track
 
+    def _smear_tables(self):
+        """cos(theta) quantile tables of the track smear: table 0 serves the
+        Cherenkov emitters (the default Beta or the `track_smear` override),
+        then one per distinct Beta(a, b) of ExtendedCherenkovEmitterCustomSmear
+        sources; and the table index of every source."""
+        from .track_smear import beta_track_quantiles
+        tables = [np.asarray(self.track_quantiles(), np.float32)]
+        keys = {}
+        index = []
+        for s in self.sources:
+            if isinstance(s, _sources.ExtendedCherenkovEmitterCustomSmear):
+                key = (float(s.cherenkov_beta_a), float(s.cherenkov_beta_b))
+                if key not in keys:
+                    q = beta_track_quantiles(*key, n=len(tables[0]))
+                    if np.array_equal(q, tables[0]):
+                        keys[key] = 0
+                    else:
+                        keys[key] = len(tables)
+                        tables.append(q)
+                index.append(keys[key])
+            else:
+                index.append(0)
+        return np.stack(tables), index
+
+    def track_table_stack(self) -> np.ndarray:
+        """(n_tables, n_knots) float32 quantile tables for pp_set_track_smear_tables."""
+        return self._smear_tables()[0]
+
     def source_records(self):
-        return _sources.to_records(self.sources)
+        recs = _sources.to_records(self.sources)
+        if self.needs_track_smear():
+            for i, t in enumerate(self._smear_tables()[1]):
+                recs[i].smear_table = t
+        return recs
 
     def sphere_records(self):
         return _targets.to_spheres(self.targets)
@@ -89,7 +121,7 @@ class PhotonPropSetup:
         else:
             ctx.set_monochromatic(self.mono_wavelength)
         if self.needs_track_smear():
-            ctx.set_track_smear(self.track_quantiles())
+            ctx.set_track_smear_tables(self.track_table_stack())
         if self.has_shaped_targets():
             ctx.set_shaped_targets(self.target_records(), self.n_target_records())
         else:

@@ -183,6 +183,17 @@ class ExtendedCherenkovEmitterNoSmear(ExtendedCherenkovEmitter):
 
 
 @dataclass
+class ExtendedCherenkovEmitterCustomSmear(ExtendedCherenkovEmitter):
+    """The cascade emitter with the track direction's cos(theta) drawn as
+    2 Beta(cherenkov_beta_a, cherenkov_beta_b) - 1 (src/lightyield.jl:725-769;
+    src/photon_prop_cuda.jl:134-154, 238-250).  The device samples it from a
+    quantile table of that Beta distribution (one table per distinct (a, b),
+    pp_set_track_smear_tables)."""
+    cherenkov_beta_a: float = 1.776
+    cherenkov_beta_b: float = 0.164
+
+
+@dataclass
 class PointlikeCherenkovEmitter(_CherenkovBase):
     """src/lightyield.jl PointlikeCherenkovEmitter; src/photon_prop_cuda.jl:254-263."""
     position: Sequence[float]

@@ -94,6 +94,9 @@ EMITTERS = {
         [3.0, -2.0, 1.0], [0.6, 0.0, 0.8], 0.0, 200_000, pp.LongitudinalParameterisation(2.0, 0.63, 0.36)),
     "extended_cherenkov_nosmear": lambda pp: pp.ExtendedCherenkovEmitterNoSmear(
         [3.0, -2.0, 1.0], [0.0, 0.6, 0.8], 5.0, 200_000, pp.LongitudinalParameterisation(0.7, 0.63, 0.36)),
+    "custom_smear": lambda pp: pp.ExtendedCherenkovEmitterCustomSmear(
+        [3.0, -2.0, 1.0], [0.6, 0.0, 0.8], 0.0, 200_000, pp.LongitudinalParameterisation(2.0, 0.63, 0.36),
+        3.0, 0.4),
     "pointlike_cherenkov": lambda pp: pp.PointlikeCherenkovEmitter(
         [0.0, 0.0, 0.0], [0.0, 0.0, 1.0], 0.0, 200_000),
     "cherenkov_track": lambda pp: pp.CherenkovTrackEmitter(
@@ -118,6 +121,30 @@ def test_emitter_replay(pp, orc, gpu_ctx, name):
     assert nsim == st.n_ph_sim
     s = compare(cols, oracle_columns(want), spheres_of(setup))
     assert s["matched"] > 100, s
+
+
+def test_custom_smear_tables_replay(pp, orc, gpu_ctx):
+    """Sources drawing their track smear from different tables in one launch."""
+    med = pp.CascadiaMediumProperties()
+    lp = pp.LongitudinalParameterisation(2.0, 0.63, 0.36)
+    srcs = [pp.ExtendedCherenkovEmitter([0.0, 0.0, 0.0], [0.0, 0.0, 1.0], 0.0, 150_000, lp),
+            pp.ExtendedCherenkovEmitterCustomSmear([0.0, 0.0, 0.0], [0.0, 0.0, 1.0], 0.0, 150_000,
+                                                   lp, 1e3, 1e-3),
+            pp.ExtendedCherenkovEmitterCustomSmear([0.0, 0.0, 0.0], [0.0, 0.0, 1.0], 0.0, 150_000,
+                                                   lp, 0.5, 0.5)]
+    targets = [pp.HomogeneousDetector(pp.Spherical(p, 1.0), 1.0, i + 1)
+               for i, p in enumerate([[0, 0, 10], [8, 0, 6], [-6, 5, 8], [0, -9, 4], [5, 5, -5]])]
+    setup = pp.PhotonPropSetup(srcs, targets, med, pp.make_cherenkov_spectrum((300.0, 800.0), med),
+                               5)
+    assert setup.track_table_stack().shape[0] == 3
+    rc, cols, nh, nsim = gpu_run(pp, setup, precise_math=1)
+    assert rc == 0
+    want, sim, _ = orc.Run.from_setup(setup).propagate_all()
+    assert nsim == sim == 450_000
+    s = compare(cols, oracle_columns(want), spheres_of(setup))
+    assert s["matched"] > 300, s
+    for k in range(3):
+        assert (cols["source_index"] == k).sum() > 50, k
 
 
 def test_many_sources_one_launch(pp, orc, gpu_ctx):
