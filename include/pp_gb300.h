@@ -107,17 +107,20 @@ typedef struct pp_sphere {
  * SimpleMediumProperties, src/simple_medium.jl:1-15).  The Julia shim fills
  * the tables with the reference's own scattering_length / group_velocity /
  * absorption_length / phase_refractive_index. */
+#define PP_PHASE_HG_ES 0  /* MixedHGES: HG(g) or Einstein-Smoluchowski(b) (water)       */
+#define PP_PHASE_HG_SL 1  /* HG(g) or simplified Liu(g), cos = 2 u^((1-g)/(1+g)) - 1
+                             (mixed_hg_sl_scattering_func_ppc, deep ice)              */
 typedef struct pp_medium {
   float wl_min;                       /* nm of knot 0                        */
   float wl_step;                      /* nm between knots (> 0)              */
   int32_t n_knots;                    /* >= 2                                */
-  int32_t reserved0;
+  int32_t phase_kind;                 /* PP_PHASE_*                          */
   const float* scattering_length;     /* m    [n_knots]                      */
   const float* group_velocity;        /* m/ns [n_knots]                      */
   const float* absorption_length;     /* m    [n_knots]                      */
   const float* phase_refractive_index;/*      [n_knots]                      */
   float hg_g;                         /* Henyey-Greenstein mean cosine       */
-  float es_b;                         /* Einstein-Smoluchowski b             */
+  float es_b;                         /* Einstein-Smoluchowski b (HG_ES)     */
   float hg_weight;                    /* P(HG) in the mixture; 1 = pure HG   */
   float reserved1;
 } pp_medium;

@@ -48,6 +48,10 @@ class ppo_medium(Structure):
         ("abs_wl", POINTER(c_double)), ("abs_len", POINTER(c_double)),
         ("s_sca_len", c_double), ("s_abs_len", c_double), ("s_ref_index", c_double),
         ("s_group_velocity", c_double),
+        ("i_a_dust_400", c_double), ("i_b_dust_400", c_double), ("i_alpha_sca_dust", c_double),
+        ("i_kappa_abs_dust", c_double), ("i_A", c_double), ("i_B", c_double),
+        ("i_delta_t", c_double), ("i_mean_cos", c_double),
+        ("phase_kind", c_int32), ("reserved_phase", c_int32),
     ]
 
 
@@ -96,7 +100,8 @@ def load():
         L.ppo_dispersion_f64.restype = c_double
         L.ppo_dispersion_f64.argtypes = [POINTER(ppo_medium), c_double]
         for n, t in (("ppo_hg_cos_f64", c_double), ("ppo_es_cos_f64", c_double),
-                     ("ppo_hg_cos_f32", c_float), ("ppo_es_cos_f32", c_float)):
+                     ("ppo_hg_cos_f32", c_float), ("ppo_es_cos_f32", c_float),
+                     ("ppo_sl_cos_f64", c_double), ("ppo_sl_cos_f32", c_float)):
             getattr(L, n).restype = t
             getattr(L, n).argtypes = [t, t]
         L.ppo_rot_from_ez_f64.argtypes = [dp, dp, dp]

@@ -131,7 +131,43 @@ static double abs_interp_f64(const ppo_medium* m, double wl) {
   return m->abs_len[lo] + f * (m->abs_len[hi] - m->abs_len[lo]);
 }
 
+/* Deep ice (src/ice_properties.jl:108-176): phase index polynomial in
+ * wl/1000, group index = n times a second polynomial, absorption = SPICE dust
+ * a_dust (wl/400)^-kappa plus A exp(-B/wl) (1 + 0.01 dT), scattering =
+ * b_dust (wl/400)^-alpha / (1 - <cos>). */
+static void ice_eval_f64(const ppo_medium* m, double wl, double out[4]) {
+  double x = wl / 1000.0;
+  double n = 1.55749 - 1.57988 * x + 3.99993 * x * x - 4.68271 * x * x * x +
+             2.09354 * x * x * x * x;
+  double ng = n * (1.0 + 0.227106 - 0.954648 * x + 1.42568 * x * x - 0.711832 * x * x * x);
+  double a = m->i_a_dust_400 * pow(wl / 400.0, -m->i_kappa_abs_dust) +
+             m->i_A * exp(-m->i_B / wl) * (1.0 + 0.01 * m->i_delta_t);
+  double b = m->i_b_dust_400 * pow(wl / 400.0, -m->i_alpha_sca_dust) / (1.0 - m->i_mean_cos);
+  out[0] = 1.0 / b * m->sca_scale;
+  out[1] = C_VAC_M_NS / ng;
+  out[2] = 1.0 / a * m->abs_scale;
+  out[3] = n;
+}
+static void ice_eval_f32(const ppo_medium* m, float wl, float out[4]) {
+  float x = wl / 1000.0f;
+  float n = 1.55749f - 1.57988f * x + 3.99993f * x * x - 4.68271f * x * x * x +
+            2.09354f * x * x * x * x;
+  float ng = n * (1.0f + 0.227106f - 0.954648f * x + 1.42568f * x * x - 0.711832f * x * x * x);
+  float a = (float)m->i_a_dust_400 * powf(wl / 400.0f, -(float)m->i_kappa_abs_dust) +
+            (float)m->i_A * expf(-(float)m->i_B / wl) * (1.0f + 0.01f * (float)m->i_delta_t);
+  float b = (float)m->i_b_dust_400 * powf(wl / 400.0f, -(float)m->i_alpha_sca_dust) /
+            (1.0f - (float)m->i_mean_cos);
+  out[0] = 1.0f / b * (float)m->sca_scale;
+  out[1] = (float)C_VAC_M_NS / ng;
+  out[2] = 1.0f / a * (float)m->abs_scale;
+  out[3] = n;
+}
+
 void ppo_medium_eval_f64(const ppo_medium* m, double wl, double out[4]) {
+  if (m->kind == PPO_MEDIUM_ICE) {
+    ice_eval_f64(m, wl, out);
+    return;
+  }
   if (m->kind == PPO_MEDIUM_SIMPLE) { /* src/simple_medium.jl:11-15 */
     out[0] = m->s_sca_len;
     out[1] = m->s_group_velocity;
@@ -149,6 +185,10 @@ void ppo_medium_eval_f64(const ppo_medium* m, double wl, double out[4]) {
 }
 
 void ppo_medium_eval_f32(const ppo_medium* m, float wl, float out[4]) {
+  if (m->kind == PPO_MEDIUM_ICE) {
+    ice_eval_f32(m, wl, out);
+    return;
+  }
   if (m->kind == PPO_MEDIUM_SIMPLE) {
     out[0] = (float)m->s_sca_len;
     out[1] = (float)m->s_group_velocity;
@@ -190,6 +230,15 @@ float ppo_es_cos_f32(float b, float eta) {
   float q = (b + 3.0f) * (eta - 0.5f) / b;
   float d = sqrtf(q * q + 1.0f / (b * b * b));
   return cbrtf(q + d) + cbrtf(q - d);
+}
+
+/* Simplified Liu inverse CDF (the SL half of mixed_hg_sl_scattering_func_ppc,
+ * CherenkovMediumBase 1.0.0, as PPC samples it). */
+double ppo_sl_cos_f64(double g, double eta) {
+  return 2.0 * pow(eta, (1.0 - g) / (1.0 + g)) - 1.0;
+}
+float ppo_sl_cos_f32(float g, float eta) {
+  return 2.0f * powf(eta, (1.0f - g) / (1.0f + g)) - 1.0f;
 }
 
 /* ---------------- geometry (PhysicsTools) ---------------------------------- */

@@ -46,6 +46,7 @@ extern "C" {
  * scattering_length / group_velocity at src/photon_prop_cuda.jl:480-482). */
 #define PPO_MEDIUM_CASCADIA 0 /* src/water_properties.jl:43-100 */
 #define PPO_MEDIUM_SIMPLE 1   /* src/simple_medium.jl:1-15      */
+#define PPO_MEDIUM_ICE 2      /* src/ice_properties.jl:26-176   */
 
 typedef struct ppo_medium {
   int32_t kind;
@@ -58,6 +59,12 @@ typedef struct ppo_medium {
   const double* abs_len;     /* m                                           */
   /* SIMPLE medium constants */
   double s_sca_len, s_abs_len, s_ref_index, s_group_velocity;
+  /* ICE (HomogenousIceProperties): SPICE dust coefficients at 400 nm and
+   * exponents, the A/B/delta-T pure-ice absorption terms, mean cos */
+  double i_a_dust_400, i_b_dust_400, i_alpha_sca_dust, i_kappa_abs_dust;
+  double i_A, i_B, i_delta_t, i_mean_cos;
+  int32_t phase_kind; /* PP_PHASE_HG_ES or PP_PHASE_HG_SL */
+  int32_t reserved_phase;
 } ppo_medium;
 
 /* One oracle hit (all fields widened to double). */
@@ -127,6 +134,9 @@ double ppo_hg_cos_f64(double g, double eta);
 float ppo_hg_cos_f32(float g, float eta);
 double ppo_es_cos_f64(double b, double eta);
 float ppo_es_cos_f32(float b, float eta);
+/* Simplified Liu, p(x) ~ (1 + x)^(2g/(1-g)): x = 2 eta^((1-g)/(1+g)) - 1. */
+double ppo_sl_cos_f64(double g, double eta);
+float ppo_sl_cos_f32(float g, float eta);
 
 /* Rotation taking e_z onto unit vector a, applied to b. */
 void ppo_rot_from_ez_f64(const double a[3], const double b[3], double out[3]);

@@ -52,9 +52,13 @@ class pp_sphere(Structure):
     _fields_ = [("position", c_float * 3), ("radius", c_float)]
 
 
+PP_PHASE_HG_ES = 0
+PP_PHASE_HG_SL = 1
+
+
 class pp_medium(Structure):
     _fields_ = [
-        ("wl_min", c_float), ("wl_step", c_float), ("n_knots", c_int32), ("reserved0", c_int32),
+        ("wl_min", c_float), ("wl_step", c_float), ("n_knots", c_int32), ("phase_kind", c_int32),
         ("scattering_length", POINTER(c_float)), ("group_velocity", POINTER(c_float)),
         ("absorption_length", POINTER(c_float)), ("phase_refractive_index", POINTER(c_float)),
         ("hg_g", c_float), ("es_b", c_float), ("hg_weight", c_float), ("reserved1", c_float),

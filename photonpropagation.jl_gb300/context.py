@@ -111,6 +111,7 @@ class Context:
         m.absorption_length = arrs[2].ctypes.data_as(fp)
         m.phase_refractive_index = arrs[3].ctypes.data_as(fp)
         m.hg_g, m.es_b, m.hg_weight = t.hg_g, t.es_b, t.hg_weight
+        m.phase_kind = int(getattr(t, "phase_kind", 0))
         check(self._lib.pp_set_medium(self.ptr, byref(m)), "pp_set_medium")
 
     def set_spectrum(self, knots) -> None:

@@ -416,12 +416,8 @@ PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
   if (!m->scattering_length || !m->group_velocity || !m->absorption_length ||
       !m->phase_refractive_index)
     return set_error(PP_ERR_INVALID, "medium table pointer is null");
-  if (!(m->hg_weight >= 0.0f && m->hg_weight <= 1.0f))
-    return set_error(PP_ERR_INVALID, "hg_weight must be in [0, 1]");
-  if (m->hg_weight > 0.0f && !(fabsf(m->hg_g) >= 1e-3f && fabsf(m->hg_g) < 1.0f))
-    return set_error(PP_ERR_INVALID, "hg_g must satisfy 1e-3 <= |g| < 1");
-  if (m->hg_weight < 1.0f && !(m->es_b > 0.0f))
-    return set_error(PP_ERR_INVALID, "es_b must be > 0 when the ES component is used");
+  pp::PhaseDev phase{};
+  if (const char* why = pp::make_phase(m, &phase)) return set_error(PP_ERR_INVALID, "%s", why);
   std::vector<float4> t(m->n_knots);
   for (int i = 0; i < m->n_knots; ++i) {
     const float s = m->scattering_length[i], v = m->group_velocity[i];
@@ -440,16 +436,7 @@ PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
   ctx->n_medium = m->n_knots;
   ctx->med_wl_min = m->wl_min;
   ctx->med_inv_step = 1.0f / m->wl_step;
-  pp::PhaseDev& p = ctx->phase;
-  p.hg_weight = m->hg_weight;
-  p.hg_g = m->hg_g;
-  p.hg_1mg2 = 1.0f - m->hg_g * m->hg_g;
-  p.hg_1pg2 = 1.0f + m->hg_g * m->hg_g;
-  p.hg_inv2g = m->hg_weight > 0.0f ? 1.0f / (2.0f * m->hg_g) : 0.0f;
-  const float b = m->es_b > 0.0f ? m->es_b : 1.0f;
-  p.es_k1 = (b + 3.0f) / b;
-  p.es_k2 = 1.0f / (b * b * b);
-  p.es_b = b;
+  ctx->phase = phase;
   ctx->has_medium = true;
   ctx->version++;
   return PP_OK;

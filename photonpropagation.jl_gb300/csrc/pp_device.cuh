@@ -205,28 +205,39 @@ __device__ __forceinline__ float4 medium_at(const float4* __restrict__ t, int n,
 }
 
 // ---- scattering (update_direction, src/photon_prop_cuda.jl:280-298) ---------
-// MixedHGES: with probability hg_weight Henyey-Greenstein at g, else
-// Einstein-Smoluchowski at b (Cardano root of the cubic CDF).  Both samples
-// are computed and one is selected (a warp almost always needs both anyway).
+// With probability hg_weight Henyey-Greenstein at g, else the second
+// component: Einstein-Smoluchowski at b (MixedHGES, Cardano root of the cubic
+// CDF) or simplified Liu at g (cos = 2 eta^((1-g)/(1+g)) - 1, the deep-ice
+// mixture).  Both samples are computed and one is selected (a warp almost
+// always needs both anyway); the second component's kind is uniform per
+// launch.
 template <bool P>
 __device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_choice, float eta) {
-  float hg, es;
-  if (P) {  // the oracle's expression forms, IEEE division/sqrt/cbrt
+  float hg, other;
+  if (P) {  // the oracle's expression forms, IEEE division/sqrt/cbrt/pow
     const float g = ph.hg_g, b = ph.es_b;
     const float t = (1.0f - g * g) / (1.0f + g * (2.0f * eta - 1.0f));
     hg = 1.0f / (2.0f * g) * (1.0f + g * g - t * t);
     hg = hg < -1.0f ? -1.0f : (hg > 1.0f ? 1.0f : hg);
-    const float q = (b + 3.0f) * (eta - 0.5f) / b;
-    const float d = sqrtf(q * q + 1.0f / (b * b * b));
-    es = cbrtf(q + d) + cbrtf(q - d);
+    if (ph.kind == PP_PHASE_HG_SL) {
+      other = 2.0f * powf(eta, ph.sl_exp) - 1.0f;
+    } else {
+      const float q = (b + 3.0f) * (eta - 0.5f) / b;
+      const float d = sqrtf(q * q + 1.0f / (b * b * b));
+      other = cbrtf(q + d) + cbrtf(q - d);
+    }
   } else {
     const float t = ph.hg_1mg2 * approx_rcp(fmaf(ph.hg_g, 2.0f * eta - 1.0f, 1.0f));
     hg = fminf(fmaxf((ph.hg_1pg2 - t * t) * ph.hg_inv2g, -1.0f), 1.0f);
-    const float q = ph.es_k1 * (eta - 0.5f);
-    const float d = approx_sqrt(fmaf(q, q, ph.es_k2));
-    es = f_cbrt_pos<false>(q + d) - f_cbrt_pos<false>(d - q);
+    if (ph.kind == PP_PHASE_HG_SL) {
+      other = fmaf(2.0f, approx_ex2(ph.sl_exp * approx_lg2(eta)), -1.0f);
+    } else {
+      const float q = ph.es_k1 * (eta - 0.5f);
+      const float d = approx_sqrt(fmaf(q, q, ph.es_k2));
+      other = f_cbrt_pos<false>(q + d) - f_cbrt_pos<false>(d - q);
+    }
   }
-  return u_choice < ph.hg_weight ? hg : es;
+  return u_choice < ph.hg_weight ? hg : other;
 }
 
 template <bool P>

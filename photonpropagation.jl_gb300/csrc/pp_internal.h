@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -80,7 +81,36 @@ struct PhaseDev {
   float es_k1;      // (b + 3) / b
   float es_k2;      // 1 / b^3
   float es_b;       // Einstein-Smoluchowski b
+  int kind;         // PP_PHASE_*
+  float sl_exp;     // simplified Liu: (1 - g) / (1 + g)
 };
+
+// The phase function of a medium, validated: nullptr on success, else the
+// reason.  Shared by pp_set_medium and pp_propagate_static.
+inline const char* make_phase(const pp_medium* m, PhaseDev* p) {
+  if (m->phase_kind != PP_PHASE_HG_ES && m->phase_kind != PP_PHASE_HG_SL)
+    return "phase_kind must be PP_PHASE_HG_ES or PP_PHASE_HG_SL";
+  if (!(m->hg_weight >= 0.0f && m->hg_weight <= 1.0f)) return "hg_weight must be in [0, 1]";
+  const float g = m->hg_g;
+  if (m->hg_weight > 0.0f && !(std::fabs(g) >= 1e-3f && std::fabs(g) < 1.0f))
+    return "hg_g must satisfy 1e-3 <= |g| < 1";
+  if (m->phase_kind == PP_PHASE_HG_ES && m->hg_weight < 1.0f && !(m->es_b > 0.0f))
+    return "es_b must be > 0 when the ES component is used";
+  if (m->phase_kind == PP_PHASE_HG_SL && m->hg_weight < 1.0f && !(g > -1.0f && g < 1.0f))
+    return "the simplified-Liu component needs -1 < g < 1";
+  const float b = m->es_b > 0.0f ? m->es_b : 1.0f;
+  p->hg_weight = m->hg_weight;
+  p->hg_g = g;
+  p->hg_1mg2 = 1.0f - g * g;
+  p->hg_1pg2 = 1.0f + g * g;
+  p->hg_inv2g = m->hg_weight > 0.0f ? 1.0f / (2.0f * g) : 0.0f;
+  p->es_k1 = (b + 3.0f) / b;
+  p->es_k2 = 1.0f / (b * b * b);
+  p->es_b = b;
+  p->kind = m->phase_kind;
+  p->sl_exp = (1.0f - g) / (1.0f + g);
+  return nullptr;
+}
 
 // Everything one launch of the propagation kernel needs (kernel parameter,
 // passed as __grid_constant__).

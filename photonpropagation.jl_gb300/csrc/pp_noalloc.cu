@@ -187,10 +187,8 @@ extern "C" PP_API int pp_propagate_static(
   if (medium->n_knots < 2 || !(medium->wl_step > 0.0f) || !medium->scattering_length ||
       !medium->group_velocity || !medium->absorption_length || !medium->phase_refractive_index)
     return fail(PP_ERR_INVALID, "medium needs n_knots >= 2, wl_step > 0 and four tables");
-  if (!(medium->hg_weight >= 0.0f && medium->hg_weight <= 1.0f) ||
-      (medium->hg_weight > 0.0f && !(std::fabs(medium->hg_g) >= 1e-3f && std::fabs(medium->hg_g) < 1.0f)) ||
-      (medium->hg_weight < 1.0f && !(medium->es_b > 0.0f)))
-    return fail(PP_ERR_INVALID, "invalid phase-function parameters");
+  pp::PhaseDev phase{};
+  if (const char* why = pp::make_phase(medium, &phase)) return fail(PP_ERR_INVALID, why);
   if (n_spectrum < 0 || (n_spectrum > 0 && !spectrum_knots) ||
       (n_spectrum == 0 && !(mono_wavelength > 0.0f)))
     return fail(PP_ERR_INVALID, "spectrum: pass knots or a positive monochromatic wavelength");
@@ -319,15 +317,7 @@ extern "C" PP_API int pp_propagate_static(
   a.n_medium = medium->n_knots;
   a.med_wl_min = medium->wl_min;
   a.med_inv_step = 1.0f / medium->wl_step;
-  const float g = medium->hg_g, b = medium->es_b > 0.0f ? medium->es_b : 1.0f;
-  a.phase.hg_weight = medium->hg_weight;
-  a.phase.hg_g = g;
-  a.phase.hg_1mg2 = 1.0f - g * g;
-  a.phase.hg_1pg2 = 1.0f + g * g;
-  a.phase.hg_inv2g = medium->hg_weight > 0.0f ? 1.0f / (2.0f * g) : 0.0f;
-  a.phase.es_k1 = (b + 3.0f) / b;
-  a.phase.es_k2 = 1.0f / (b * b * b);
-  a.phase.es_b = b;
+  a.phase = phase;
   a.spectrum = n_spectrum > 0 ? d_spec : nullptr;
   a.n_spectrum = n_spectrum;
   a.mono_wavelength = mono_wavelength;

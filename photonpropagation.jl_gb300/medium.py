@@ -22,6 +22,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _lib
+
 C_VAC_M_NS = 0.299792458
 
 _DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
@@ -70,6 +72,7 @@ class MediumTables:
     hg_g: float
     es_b: float
     hg_weight: float
+    phase_kind: int = 0  # PP_PHASE_HG_ES / PP_PHASE_HG_SL
 
     @property
     def n_knots(self) -> int:
@@ -116,7 +119,8 @@ class MediumProperties:
             group_velocity=np.asarray(self.group_velocity(wl), np.float32),
             absorption_length=np.asarray(self.absorption_length(wl), np.float32),
             phase_refractive_index=np.asarray(self.phase_refractive_index(wl), np.float32),
-            hg_g=float(self.hg_g), es_b=float(self.es_b), hg_weight=float(self.hg_weight))
+            hg_g=float(self.hg_g), es_b=float(self.es_b), hg_weight=float(self.hg_weight),
+            phase_kind=int(getattr(self, "phase_kind", 0)))
 
     def oracle_params(self) -> dict:
         raise NotImplementedError
@@ -231,3 +235,92 @@ class SimpleMediumProperties(MediumProperties):
                     s_sca_len=self.scattering_length_m, s_abs_len=self.absorption_length_m,
                     s_ref_index=self.phase_refractive_index_value,
                     s_group_velocity=self.group_velocity_m_ns)
+
+
+class HomogenousIceProperties(MediumProperties):
+    """Deep homogeneous ice with the SPICE model (src/ice_properties.jl:26-176).
+
+    ``HomogenousIceProperties(radiation_length=..., mean_scattering_angle=...,
+    hg_fraction=..., A_SPICE=..., B_SPICE=..., D_SPICE=..., E_SPICE=...,
+    a_dust_400=..., b_dust_400=..., alpha_sca_dust=..., kappa_abs_dust=...,
+    deltaTSPICE=..., abs_scale=..., sca_scale=...)`` with the reference's keyword
+    names (stored as FP32, the device's precision).  Phase function:
+    Henyey-Greenstein at the mean cosine g with probability ``hg_fraction``,
+    else simplified Liu at g (cos = 2 u^((1-g)/(1+g)) - 1), the mixture of
+    ``mixed_hg_sl_scattering_func_ppc`` (CherenkovMediumBase 1.0.0, absent
+    here) with ``hg_fraction`` read as the HG weight, as the field's docstring
+    says.  Both components have mean cosine g."""
+
+    phase_kind = _lib.PP_PHASE_HG_SL
+    es_b = 0.0
+
+    def __init__(self, radiation_length, mean_scattering_angle, hg_fraction, A_SPICE, B_SPICE,
+                 D_SPICE, E_SPICE, a_dust_400, b_dust_400, alpha_sca_dust, kappa_abs_dust,
+                 deltaTSPICE, abs_scale=1.0, sca_scale=1.0):
+        f32 = lambda x: float(np.float32(x))  # noqa: E731
+        self.radiation_length_gcm2 = f32(radiation_length)
+        self.hg_g = f32(mean_scattering_angle)
+        self.hg_weight = f32(hg_fraction)
+        self.A_SPICE, self.B_SPICE = f32(A_SPICE), f32(B_SPICE)
+        self.D_SPICE, self.E_SPICE = f32(D_SPICE), f32(E_SPICE)
+        self.a_dust_400, self.b_dust_400 = f32(a_dust_400), f32(b_dust_400)
+        self.alpha_sca_dust, self.kappa_abs_dust = f32(alpha_sca_dust), f32(kappa_abs_dust)
+        self.deltaTSPICE = f32(deltaTSPICE)
+        self.abs_scale, self.sca_scale = f32(abs_scale), f32(sca_scale)
+
+    def mean_scattering_angle(self) -> float:
+        return self.hg_g
+
+    def radiation_length(self) -> float:
+        return self.radiation_length_gcm2
+
+    def material_density(self) -> float:
+        return 0.910 * 1000  # src/ice_properties.jl:91
+
+    def phase_refractive_index(self, wl):
+        """Polynomial in wl/1000 (src/ice_properties.jl:98-107)."""
+        x = np.asarray(wl, np.float64) / 1000.0
+        return 1.55749 - 1.57988 * x + 3.99993 * x ** 2 - 4.68271 * x ** 3 + 2.09354 * x ** 4
+
+    def group_refractive_index(self, wl):
+        """n times a second polynomial in wl/1000 (src/ice_properties.jl:110-121)."""
+        x = np.asarray(wl, np.float64) / 1000.0
+        return self.phase_refractive_index(wl) * (1 + 0.227106 - 0.954648 * x + 1.42568 * x ** 2
+                                                  - 0.711832 * x ** 3)
+
+    def group_velocity(self, wl):
+        return C_VAC_M_NS / self.group_refractive_index(wl)
+
+    def absorption_length(self, wl):
+        """1 / (a_dust (wl/400)^-kappa + A exp(-B/wl) (1 + 0.01 dT)), scaled
+        (src/ice_properties.jl:131-160)."""
+        wl = np.asarray(wl, np.float64)
+        a = (self.a_dust_400 * (wl / 400.0) ** (-self.kappa_abs_dust) +
+             self.A_SPICE * np.exp(-self.B_SPICE / wl) * (1 + 0.01 * self.deltaTSPICE))
+        return 1.0 / a * self.abs_scale
+
+    def scattering_length(self, wl):
+        """(1 - g) / (b_dust (wl/400)^-alpha), scaled (src/ice_properties.jl:162-174)."""
+        wl = np.asarray(wl, np.float64)
+        eff = self.b_dust_400 * (wl / 400.0) ** (-self.alpha_sca_dust)
+        return 1.0 / (eff / (1 - self.hg_g)) * self.sca_scale
+
+    def oracle_params(self) -> dict:
+        return dict(kind=2, hg_g=self.hg_g, es_b=0.0, hg_weight=self.hg_weight,
+                    abs_scale=self.abs_scale, sca_scale=self.sca_scale,
+                    i_a_dust_400=self.a_dust_400, i_b_dust_400=self.b_dust_400,
+                    i_alpha_sca_dust=self.alpha_sca_dust, i_kappa_abs_dust=self.kappa_abs_dust,
+                    i_A=self.A_SPICE, i_B=self.B_SPICE, i_delta_t=self.deltaTSPICE,
+                    i_mean_cos=self.hg_g, phase_kind=int(_lib.PP_PHASE_HG_SL))
+
+
+def make_homogenous_clearice_properties(T=None, abs_scale=1.0, sca_scale=1.0):
+    """The "homogeneous clear ice" model (src/ice_properties.jl:49-64); the
+    element type T of the reference is accepted and ignored (FP32 on the device)."""
+    return HomogenousIceProperties(
+        radiation_length=39.652 / 0.9216, mean_scattering_angle=0.9, hg_fraction=0.45,
+        A_SPICE=6954.090332031250, B_SPICE=6617.754394531250, D_SPICE=0.0, E_SPICE=0.0,
+        a_dust_400=0.006350013, b_dust_400=0.02331206666666667, alpha_sca_dust=0.898608505726,
+        kappa_abs_dust=1.084106802940, deltaTSPICE=12.115215000000001, abs_scale=abs_scale,
+        sca_scale=sca_scale)
+
