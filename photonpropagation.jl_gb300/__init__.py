@@ -21,7 +21,7 @@ from .sources import (AxiconeEmitter, CherenkovTrackEmitter, CollimatedIsotropic
                       LongitudinalParameterisation, PencilEmitter, PointlikeCherenkovEmitter,
                       PointlikeIsotropicEmitter, PointlikeTimeRangeEmitter, source_photons)
 from .spectrum import (InterpolatedSpectralDist, Monochromatic, Spectrum, frank_tamm,
-                       make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
+                       make_biased_cherenkov_spectrum, make_cherenkov_spectrum, make_monochromatic_spectrum, make_spectral_dist)
 from .targets import (Circular, DetectorLine, DetectorLines, HomogeneousDetector, Rectangular,
                       Spherical)
 from . import calc, detection, dom, generic_multipmt, particles, pom, surrogate, workloads

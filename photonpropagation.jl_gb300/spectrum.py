@@ -100,6 +100,15 @@ def make_cherenkov_spectrum(wl_range, medium) -> Spectrum:
                     (float(wl_range[0]), float(wl_range[1])))
 
 
+def make_biased_cherenkov_spectrum(bias_function: Callable, wl_range, medium) -> Spectrum:
+    """Frank-Tamm spectrum times `bias_function(wl)` (e.g. a module's wavelength
+    acceptance), its CDF tabulated every 0.5 nm (src/spectrum.jl:97-101)."""
+    def sfunc(wl):
+        return frank_tamm(wl, medium.phase_refractive_index(wl)) * bias_function(wl) * 1e9
+    return Spectrum(make_spectral_dist(sfunc, wl_range, 0.5), sfunc,
+                    (float(wl_range[0]), float(wl_range[1])))
+
+
 def make_monochromatic_spectrum(wl: float) -> Spectrum:
     """src/spectrum.jl:103-105"""
     return Spectrum(Monochromatic(float(wl)), lambda w: np.where(np.asarray(w) == wl, 1.0, 0.0),

@@ -112,3 +112,26 @@ def test_ice_replay(pp, orc, gpu_ctx):
     assert nsim == sim == 200_000
     s = compare(got, oracle_columns(want), spheres_of(setup))
     assert s["matched"] > 1000, s
+
+
+def test_biased_cherenkov_spectrum(pp):
+    """Frank-Tamm times a DOM's wavelength acceptance (the reference's example
+    pattern): its CDF at the 0.5 nm knots follows the product, and the device
+    table draws no wavelength where the bias is 0 (above 680 nm)."""
+    med = pp.make_homogenous_clearice_properties()
+    bias = pp.DOM.at([0.0, 0.0, 0.0], 1).acceptance.wavelength
+    spec = pp.make_biased_cherenkov_spectrum(bias, (300.0, 800.0), med)
+    total = integrate.quad(spec.spectrum, 300, 800, points=[680], limit=400)[0]
+    d = spec.spectral_dist
+    # (the reference's one 25-point Gauss rule over [300, wl] does not resolve the
+    # acceptance table's 10 nm kinks: its CDF is off by up to ~0.3 %, reproduced here)
+    for wl in (350.0, 420.0, 500.0, 600.0, 675.0):
+        want = integrate.quad(spec.spectrum, 300, wl, limit=400)[0] / total
+        assert np.interp(wl, d.wavelengths, d.cdf) == pytest.approx(want, abs=5e-3), wl
+    knots = d.device_knots(600)
+    assert knots.min() >= 300.0 and knots.max() <= 681.0, knots.max()
+    flat = pp.make_biased_cherenkov_spectrum(lambda wl: np.ones_like(np.asarray(wl, float)),
+                                             (300.0, 800.0), med)
+    np.testing.assert_allclose(flat.spectral_dist.device_knots(600),
+                               pp.make_cherenkov_spectrum((300.0, 800.0), med)
+                               .spectral_dist.device_knots(600), atol=0.05)
