@@ -121,6 +121,8 @@ def load():
             getattr(L, n).argtypes = [POINTER(ppo_run), c_int32, c_int64, c_int64, c_void_p,
                                       c_int64, c_int32, POINTER(ppo_stats)]
         L.ppo_max_threads.restype = c_int32
+        L.ppo_abi_layout.restype = c_int64
+        L.ppo_abi_layout.argtypes = [ctypes.c_char_p]
         _L = L
     return _L
 

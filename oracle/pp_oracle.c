@@ -402,3 +402,25 @@ int32_t ppo_max_threads(void) {
   return 1;
 #endif
 }
+
+#include <stddef.h>
+#include <string.h>
+
+int64_t ppo_abi_layout(const char* what) {
+#define PPO_SIZE(T) if (!strcmp(what, #T)) return (int64_t)sizeof(T);
+#define PPO_OFF(T, f) if (!strcmp(what, #T "." #f)) return (int64_t)offsetof(T, f);
+  PPO_SIZE(pp_source) PPO_SIZE(pp_sphere) PPO_SIZE(pp_medium) PPO_SIZE(pp_tuning)
+  PPO_SIZE(pp_hit_record) PPO_SIZE(pp_counters) PPO_SIZE(pp_target) PPO_SIZE(pp_pmt_target)
+  PPO_SIZE(pp_pom_model) PPO_SIZE(pp_dom_model) PPO_SIZE(pp_multipmt_model)
+  PPO_SIZE(pp_detection_models) PPO_SIZE(pp_hits)
+  PPO_OFF(pp_source, smear_table) PPO_OFF(pp_source, first_photon)
+  PPO_OFF(pp_medium, phase_kind) PPO_OFF(pp_medium, hg_g)
+  PPO_OFF(pp_hit_record, time) PPO_OFF(pp_hit_record, module_index)
+  PPO_OFF(pp_dom_model, polymax) PPO_OFF(pp_dom_model, apply_wl_acceptance) PPO_OFF(pp_dom_model, wl)
+  PPO_OFF(pp_multipmt_model, pmt_dir) PPO_OFF(pp_multipmt_model, qe)
+  PPO_OFF(pp_pom_model, pmt_dir) PPO_OFF(pp_pom_model, pmt_group)
+  PPO_OFF(pp_detection_models, multipmt)
+#undef PPO_SIZE
+#undef PPO_OFF
+  return -1;
+}

@@ -179,6 +179,11 @@ int64_t ppo_propagate_f64(const ppo_run* run, int32_t src, int64_t begin, int64_
 /* Number of OpenMP threads available. */
 int32_t ppo_max_threads(void);
 
+/* sizeof and selected field offsets of the C-ABI structs as this C compiler
+ * lays them out from include/pp_gb300.h (checked against the ctypes mirror);
+ * -1 for an unknown name. */
+int64_t ppo_abi_layout(const char* what);
+
 #ifdef __cplusplus
 }
 #endif

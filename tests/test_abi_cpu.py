@@ -46,6 +46,61 @@ def test_struct_layouts_match_header(pp):
     assert np.dtype(L.HIT_RECORD_DTYPE).itemsize == 80
 
 
+def test_ctypes_layouts_match_the_c_compiler(pp, orc):
+    """Every ABI struct's size and the offsets the library relies on, as the C
+    compiler lays them out from the header, equal the ctypes mirror's."""
+    L = pp._lib
+    C = orc.load()
+    for name in ("pp_source", "pp_sphere", "pp_medium", "pp_tuning", "pp_hit_record",
+                 "pp_counters", "pp_target", "pp_pmt_target", "pp_pom_model", "pp_dom_model",
+                 "pp_multipmt_model", "pp_detection_models", "pp_hits"):
+        assert C.ppo_abi_layout(name.encode()) == ctypes.sizeof(getattr(L, name)), name
+    for name, field in (("pp_source", "smear_table"), ("pp_source", "first_photon"),
+                        ("pp_medium", "phase_kind"), ("pp_medium", "hg_g"),
+                        ("pp_hit_record", "time"), ("pp_hit_record", "module_index"),
+                        ("pp_dom_model", "polymax"), ("pp_dom_model", "apply_wl_acceptance"),
+                        ("pp_dom_model", "wl"), ("pp_multipmt_model", "pmt_dir"),
+                        ("pp_multipmt_model", "qe"), ("pp_pom_model", "pmt_dir"),
+                        ("pp_pom_model", "pmt_group"), ("pp_detection_models", "multipmt")):
+        got = C.ppo_abi_layout(f"{name}.{field}".encode())
+        assert got == getattr(getattr(L, name), field).offset, (name, field)
+    assert C.ppo_abi_layout(b"pp_nothing") == -1
+
+
+def test_detection_argument_checks(pp):
+    """pp_make_hits_from_photons_models rejects bad modules and models before
+    touching a device (and n = 0 is a no-op)."""
+    L = pp._lib
+    lib = L.load()
+    fake = ctypes.c_void_p(256)  # never dereferenced: validation comes first
+    tg = (L.pp_pmt_target * 1)()
+    tg[0].radius = 0.3
+
+    def call(models, n=1):
+        return lib.pp_make_hits_from_photons_models(fake, n, tg, 1, ctypes.byref(models), 0,
+                                                    fake, None, None)
+    none = L.pp_detection_models()
+    for kind, msg in ((L.PP_PMT_POM, "without its model"), (L.PP_PMT_DOM, "without its model"),
+                      (L.PP_PMT_MULTIPMT, "without its model"), (9, "unknown module kind")):
+        tg[0].kind = kind
+        assert call(none) == L.PP_ERR_INVALID and msg in L.last_error(), kind
+    tg[0].kind = L.PP_PMT_DOM
+    dom = pp.dom.dom_model()
+    dom.n_poly = 0
+    models = L.pp_detection_models(dom=ctypes.pointer(dom))
+    assert call(models) == L.PP_ERR_INVALID and "bad DOM tables" in L.last_error()
+    tg[0].kind = L.PP_PMT_MULTIPMT
+    mp = pp.generic_multipmt.multipmt_model([pp.make_generic_multipmt_om([0, 0, 0], 0.2, 1)])
+    mp.n_pmt = L.PP_MULTIPMT_MAX_PMTS + 1
+    models = L.pp_detection_models(multipmt=ctypes.pointer(mp))
+    assert call(models) == L.PP_ERR_INVALID and "bad multi-PMT tables" in L.last_error()
+    mp.n_pmt = 20
+    tg[0].radius = 0.0
+    assert call(models) == L.PP_ERR_INVALID and "radius" in L.last_error()
+    tg[0].radius = 0.2
+    assert call(models, n=0) == L.PP_OK
+
+
 def test_version_and_error_text(pp):
     lib = pp._lib.load()
     assert lib.pp_version() == 1
