@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--c3-steps", type=int, default=20000)
     ap.add_argument("--c4-pairs", type=float, default=1e6)
     ap.add_argument("--no-detection", action="store_true", help="skip the PMT detection report")
+    ap.add_argument("--detection-records", type=float, default=1e8,
+                    help="hit records of the detection report (80 B each, device-resident)")
     ap.add_argument("--surrogate-only", action="store_true",
                     help="print only the C3/C4 surrogate report (for profiling its kernels)")
     return ap.parse_args()
@@ -463,7 +465,7 @@ def bench_detection(pp, torch, local, n=100_000_000, reps=5):
     algo = 40.0  # bytes per hit: 2 x 16 B of the record read, 4 B id + 4 B QE written
     achieved = n * algo / (ms * 1e-3) / 1e9
     # CPU: the numpy oracle (one thread) on a bounded sample of the same records
-    m = 2_000_000
+    m = min(n, 2_000_000)
     host = rec[:m].cpu().numpy()
     t = pom.load_pom_tables()
     model_d = dict(acc_wavelength=t.acc_wavelength, acc_group1=t.acc_group1,
@@ -477,9 +479,9 @@ def bench_detection(pp, torch, local, n=100_000_000, reps=5):
     cpu_rate = m / (time.perf_counter() - t0)
     del rec, ids, qe, mi
     torch.cuda.empty_cache()
-    return {"workload": "1e8 hit records on 400 POMs (C1 positions), uniform on the module "
+    return {"workload": f"{n:.0e} hit records on 400 POMs (C1 positions), uniform on the module "
                         "surfaces, 1/lambda^2 wavelengths on 300-800 nm; records resident in "
-                        "HBM (8 GB)",
+                        f"HBM ({n * 80 / 1e9:.1f} GB)",
             "hits_per_s": n / (ms * 1e-3), "ms": ms, "detected_fraction": detected / n,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm if hbm else None,
@@ -603,7 +605,8 @@ def run_ours(args):
     e2e_value = e2e_photons * world / e2e_s
     c2 = None if (world > 1 or args.no_c2 or args.config != "c1") else bench_c2(pp, torch, local)
     sur = None if (world > 1 or args.no_surrogate) else bench_surrogate(pp, torch, local, args)
-    detection = None if (world > 1 or args.no_detection) else bench_detection(pp, torch, local)
+    detection = None if (world > 1 or args.no_detection) else bench_detection(
+        pp, torch, local, n=int(args.detection_records))
 
     if rank != 0:
         return 0
