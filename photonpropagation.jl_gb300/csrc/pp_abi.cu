@@ -540,7 +540,7 @@ PP_API int pp_set_shaped_targets(pp_ctx* ctx, const pp_target* t, int32_t n) {
   const bool lines = n > 0 && t[0].kind == PP_TARGET_LINE;
   const int per_line = lines ? t[0].reserved : 0;
   if (lines) {
-    if (per_line < 1 || n % (per_line + 1) != 0)
+    if (per_line < 1 || per_line >= n || n % (per_line + 1) != 0)
       return set_error(PP_ERR_INVALID, "detector lines: %d records are not groups of 1 + %d", n,
                        per_line);
     const long long n_lines = n / (per_line + 1);

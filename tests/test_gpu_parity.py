@@ -250,3 +250,28 @@ def test_photon_steps_counter(pp, orc, gpu_ctx):
     _, st = orc.Run.from_setup(setup).propagate()
     assert int(c[1]) == st.n_ph_sim
     assert abs(int(c[2]) - st.photon_steps) <= 15 * 5  # grazing hits may differ
+
+
+def test_validation_formula(pp, gpu_ctx):
+    """The reference's loose check (examples/validation.jl:300-306): photons
+    from an isotropic source reaching a sphere of radius r at distance d follow
+    norm * N r^2 / (4 d^2) * exp(-d / L) -- fitted here over five distances
+    (absorption-weighted counts, as the reference's sphere hits)."""
+    med = pp.CascadiaMediumProperties()
+    dists = np.array([8.0, 15.0, 25.0, 40.0, 60.0])
+    dirs = np.array([[0, 0, 1], [1, 0, 0], [0, 1, 0], [-1, 0, 0], [0, -1, 0]], float)
+    targets = [pp.HomogeneousDetector(pp.Spherical(list(d * u), 1.0), 1.0, i + 1)
+               for i, (d, u) in enumerate(zip(dists, dirs))]
+    n = 50_000_000
+    src = pp.PointlikeIsotropicEmitter([0.0, 0.0, 0.0], 0.0, n)
+    setup = pp.PhotonPropSetup([src], targets, med,
+                               pp.make_cherenkov_spectrum((300.0, 800.0), med), 2)
+    table = pp.propagate_photons(setup)
+    w = np.array([table["total_weight"][table["module_id"] == i + 1].sum() for i in range(5)])
+    geo = n * 1.0 / (4 * dists ** 2)
+    slope, icpt = np.polyfit(dists, np.log(w / geo), 1)
+    L, norm = -1.0 / slope, np.exp(icpt)
+    model = norm * geo * np.exp(-dists / L)
+    assert 10.0 < L < 60.0, L
+    assert 0.3 < norm < 3.0, norm
+    assert np.max(np.abs(w / model - 1)) < 0.3, w / model
