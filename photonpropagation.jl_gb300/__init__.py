@@ -33,7 +33,7 @@ from .pom import POM
 from .dom import DOM, DOMAcceptance
 from .generic_multipmt import (SphericalMultiPMTTarget, fibonacci_sphere,
                                make_generic_multipmt_om, make_generic_multipmt_positions)
-from .detection import (InterpQuantumEff, apply_qe, calc_pe_weight, check_pmt_hit_opening_angle,
-                        make_hits_from_photons)
+from .detection import (InterpQuantumEff, apply_qe, apply_wl_acceptance, calc_pe_weight,
+                        check_pmt_hit, check_pmt_hit_opening_angle, make_hits_from_photons)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

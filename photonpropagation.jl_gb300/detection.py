@@ -29,7 +29,7 @@ import numpy as np
 from . import _lib
 from ._lib import check
 from .dom import DOM, dom_model
-from .generic_multipmt import SphericalMultiPMTTarget, multipmt_model
+from .generic_multipmt import InterpQuantumEff, SphericalMultiPMTTarget, multipmt_model
 from .pom import POM, load_pom_tables, pom_model
 from .targets import HomogeneousDetector
 
@@ -42,28 +42,6 @@ def check_pmt_hit_opening_angle(rel_hit_position, pmt_positions, opening_angle) 
         if np.arccos(np.clip(rel @ p, -1.0, 1.0)) < opening_angle:
             return j + 1
     return 0
-
-
-class InterpQuantumEff:
-    """InterpQuantumEff (src/detection.jl:163-186): linear interpolation of a
-    QE table, 0 outside it; ``relative`` picks the rel_acceptance column of a
-    CSV instead of QE / 100."""
-
-    def __init__(self, wavelength, qe):
-        self.wavelength = np.asarray(wavelength, np.float64)
-        self.qe = np.asarray(qe, np.float64)
-
-    @classmethod
-    def from_csv(cls, path, relative: bool = False):
-        import csv
-        with open(path, newline="") as f:
-            rows = list(csv.DictReader(f))
-        wl = [float(r["wavelength"]) for r in rows]
-        y = [float(r["rel_acceptance"]) if relative else float(r["QE"]) / 100.0 for r in rows]
-        return cls(wl, y)
-
-    def __call__(self, wl):
-        return np.interp(np.asarray(wl, np.float64), self.wavelength, self.qe, left=0.0, right=0.0)
 
 
 def pmt_targets(targets) -> "ctypes.Array":
@@ -176,6 +154,8 @@ def apply_qe(wl, target) -> np.ndarray:
         t = load_pom_tables()
         return np.interp(wl, t.qe_wavelength, t.qe, left=0.0, right=0.0)
     if isinstance(target, SphericalMultiPMTTarget):
+        if target.wl_acceptance is None:
+            raise TypeError("apply_qe: the multi-PMT module has no wl_acceptance")
         return target.wl_acceptance(wl)
     if isinstance(target, HomogeneousDetector):
         return np.ones_like(wl)
@@ -196,3 +176,43 @@ def calc_pe_weight(table, setup_or_targets):
     table["qe_weight"] = qe
     table["total_weight"] = np.asarray(table["total_weight"], np.float64) * qe
     return table
+
+
+def check_pmt_hit(hit_positions, hit_directions, hit_wavelengths, target, orientation=None,
+                  seed: int = 0, device: int = 0) -> np.ndarray:
+    """``check_pmt_hit(positions, directions, wavelengths, target, orientation)``
+    (src/detection.jl:51-131, src/pom.jl:246-305, src/dom.jl:96-116): the 1-based
+    PMT of each photon on `target` (0 = not detected), on the device.  For a
+    DOM only the angular acceptance, as the reference (its wavelength test is
+    ``apply_wl_acceptance``)."""
+    import torch
+    pos = np.asarray(hit_positions, np.float32).reshape(-1, 3)
+    n = len(pos)
+    if n == 0:
+        return np.zeros(0, np.int32)
+    rec = np.zeros(n, dtype=np.dtype(_lib.pp_hit_record))
+    rec["position"] = pos
+    rec["direction"] = np.asarray(hit_directions, np.float32).reshape(-1, 3)
+    rec["wavelength"] = np.asarray(hit_wavelengths, np.float32).reshape(-1) \
+        if len(np.atleast_1d(hit_wavelengths)) else 0.0
+    rec["module_index"] = 1
+    d_rec = torch.from_numpy(rec.view(np.uint8)).to(f"cuda:{device}")
+    d_id = torch.empty(n, dtype=torch.int32, device=f"cuda:{device}")
+    make_hits_device(d_rec.data_ptr(), n, [target], seed, d_id.data_ptr(),
+                     orientation=orientation, apply_wl_acc=False)
+    return d_id.cpu().numpy()
+
+
+def apply_wl_acceptance(hit_positions, hit_directions, hit_wavelengths, target,
+                        orientation=None, rng=None) -> np.ndarray:
+    """``apply_wl_acceptance`` (src/dom.jl:122-134, src/pom.jl:165-174,
+    src/detection.jl:141-146): a DOM keeps a photon when u < wl_acc(wavelength);
+    POMs and multi-PMT modules keep all."""
+    wl = np.asarray(hit_wavelengths, np.float64).reshape(-1)
+    if isinstance(target, DOM):
+        rng = rng if rng is not None else np.random.default_rng()
+        return rng.uniform(size=len(wl)) < target.acceptance.wavelength(wl)
+    if isinstance(target, (POM, SphericalMultiPMTTarget)):
+        return np.ones(len(np.asarray(hit_positions).reshape(-1, 3)), bool)
+    raise NotImplementedError(f"apply_wl_acceptance not implemented for {type(target).__name__}")
+

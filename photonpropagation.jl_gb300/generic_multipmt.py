@@ -52,29 +52,48 @@ def load_multipmt_qe():
     return q[:, 0], q[:, 1]
 
 
+class InterpQuantumEff:
+    """InterpQuantumEff (src/detection.jl:163-186): linear interpolation of a
+    QE table, 0 outside it.  ``from_csv(path, relative)`` reads the reference's
+    CSV format: QE / 100, or the rel_acceptance column when ``relative``."""
+
+    def __init__(self, wavelength, qe):
+        self.wavelength = np.asarray(wavelength, np.float64)
+        self.qe = np.asarray(qe, np.float64)
+
+    @classmethod
+    def from_csv(cls, path, relative: bool = False):
+        import csv
+        with open(path, newline="") as f:
+            rows = list(csv.DictReader(f))
+        wl = [float(r["wavelength"]) for r in rows]
+        y = [float(r["rel_acceptance"]) if relative else float(r["QE"]) / 100.0 for r in rows]
+        return cls(wl, y)
+
+    def __call__(self, wl):
+        return np.interp(np.asarray(wl, np.float64), self.wavelength, self.qe, left=0.0, right=0.0)
+
+
 @dataclass
 class SphericalMultiPMTTarget:
     """SphericalMultiPMTTarget(shape, pmt_area, pmt_coordinates, wl_acceptance,
-    module_id): wl_acceptance as (wavelength, qe) knots."""
+    module_id) as NeutrinoTelescopeBase defines it: pmt_coordinates 2 x n_pmt
+    (theta; phi), wl_acceptance an InterpQuantumEff (or None, as in the
+    reference's example; calc_pe_weight then has no QE to apply)."""
     shape: Spherical
     pmt_area: float
     pmt_coordinates: np.ndarray
-    qe_wavelength: np.ndarray
-    qe: np.ndarray
+    wl_acceptance: "InterpQuantumEff | None"
     module_id: int
-
-    def wl_acceptance(self, wl):
-        return np.interp(np.asarray(wl, np.float64), self.qe_wavelength, self.qe, left=0.0,
-                         right=0.0)
 
 
 def make_generic_multipmt_om(position: Sequence[float], radius: float, module_id: int,
                              pmt_diameter: float = 0.0762) -> SphericalMultiPMTTarget:
     """make_generic_multipmt_om (src/generic_multipmt.jl:35-52)."""
-    wl, qe = load_multipmt_qe()
     return SphericalMultiPMTTarget(Spherical(list(position), float(radius)),
                                    (pmt_diameter / 2) ** 2 * np.pi,
-                                   make_generic_multipmt_positions(), wl, qe, int(module_id))
+                                   make_generic_multipmt_positions(),
+                                   InterpQuantumEff(*load_multipmt_qe()), int(module_id))
 
 
 def get_pmt_count(target: SphericalMultiPMTTarget) -> int:
@@ -90,9 +109,17 @@ def get_pmt_positions(target: SphericalMultiPMTTarget, orientation=None) -> np.n
     return d
 
 
+def _qe_knots(t: SphericalMultiPMTTarget):
+    """QE knots for the device; a target without wl_acceptance gets weight 1."""
+    if t.wl_acceptance is None:
+        return np.array([0.0, 1e4]), np.array([1.0, 1.0])
+    return t.wl_acceptance.wavelength, t.wl_acceptance.qe
+
+
 def _layout_key(t: SphericalMultiPMTTarget):
+    wl, qe = _qe_knots(t)
     return (float(t.pmt_area), np.asarray(t.pmt_coordinates, np.float64).tobytes(),
-            np.asarray(t.qe_wavelength, np.float64).tobytes(), np.asarray(t.qe, np.float64).tobytes())
+            np.asarray(wl, np.float64).tobytes(), np.asarray(qe, np.float64).tobytes())
 
 
 def multipmt_model(targets: Sequence[SphericalMultiPMTTarget],
@@ -106,19 +133,19 @@ def multipmt_model(targets: Sequence[SphericalMultiPMTTarget],
     n = get_pmt_count(t0)
     if not 1 <= n <= _lib.PP_MULTIPMT_MAX_PMTS:
         raise ValueError(f"{n} PMTs exceed the device limit {_lib.PP_MULTIPMT_MAX_PMTS}")
-    if not 2 <= len(t0.qe_wavelength) <= _lib.PP_POM_MAX_KNOTS:
+    qwl, qv = _qe_knots(t0)
+    if not 2 <= len(qwl) <= _lib.PP_POM_MAX_KNOTS:
         raise ValueError("multi-PMT QE table needs 2..128 knots")
     m = _lib.pp_multipmt_model()
     m.n_pmt = n
-    m.n_qe = len(t0.qe_wavelength)
+    m.n_qe = len(qwl)
     m.pmt_area = float(t0.pmt_area)
     dm = get_pmt_positions(t0).astype(np.float32)
     do = get_pmt_positions(t0, orientation).astype(np.float32)
     for i in range(n):
         m.pmt_dir_module[i][:] = [float(v) for v in dm[i]]
         m.pmt_dir[i][:] = [float(v) for v in do[i]]
-    for i, (x, y) in enumerate(zip(np.asarray(t0.qe_wavelength, np.float32),
-                                   np.asarray(t0.qe, np.float32))):
+    for i, (x, y) in enumerate(zip(np.asarray(qwl, np.float32), np.asarray(qv, np.float32))):
         m.qe_wavelength[i] = float(x)
         m.qe[i] = float(y)
     return m

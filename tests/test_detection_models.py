@@ -299,3 +299,56 @@ def test_make_hits_from_photons_doms_and_multipmt(pp, gpu_ctx):
     hits = pp.detection.calc_pe_weight(pp.make_hits_from_photons(
         pp.HitTable({k: v[on_mp] for k, v in table.items()}), setup, seed=5), setup)
     np.testing.assert_allclose(hits["qe_weight"], mp.wl_acceptance(hits["wavelength"]))
+
+
+def test_multipmt_as_in_the_reference_example(pp):
+    """examples/generic_multipmt_om.jl builds the module from Fibonacci points
+    with no wavelength acceptance: the device model gets QE 1, calc_pe_weight
+    has no QE to apply (the reference would fail calling nothing)."""
+    f = pp.fibonacci_sphere(20)
+    theta = np.arccos(np.clip(f[:, 2], -1, 1))
+    phi = np.arctan2(f[:, 1], f[:, 0])
+    t = pp.SphericalMultiPMTTarget(pp.Spherical([0.0, 0.0, 0.0], 0.25), (0.0762 / 2) ** 2 * np.pi,
+                                   np.stack([theta, phi]), None, 1)
+    np.testing.assert_allclose(pp.generic_multipmt.get_pmt_positions(t), f, atol=1e-12)
+    m = pp.generic_multipmt.multipmt_model([t])
+    assert m.n_pmt == 20 and (m.qe[0], m.qe[1]) == (1.0, 1.0)
+    with pytest.raises(TypeError):
+        pp.detection.apply_qe(np.array([400.0]), t)
+
+
+def test_apply_wl_acceptance(pp):
+    rng = np.random.default_rng(9)
+    dom = pp.DOM.at([0.0, 0.0, 0.0], 1)
+    wl = rng.uniform(250, 700, 200_000)
+    keep = pp.apply_wl_acceptance(np.zeros((len(wl), 3)), np.zeros((len(wl), 3)), wl, dom, rng=rng)
+    p = dom.acceptance.wavelength(wl)
+    assert abs(keep.sum() - p.sum()) < 5 * np.sqrt(p.sum())
+    assert not keep[wl > 680].any()
+    pom = pp.POM.at([0.0, 0.0, 0.0], 2)
+    assert pp.apply_wl_acceptance(np.zeros((5, 3)), np.zeros((5, 3)), [400.0] * 5, pom).all()
+
+
+@pytest.mark.gpu
+def test_check_pmt_hit_host_api(pp, gpu_ctx):
+    """check_pmt_hit for one module runs the device kernel: its decisions are
+    the oracle's for module index 1 (for a DOM the angular test only)."""
+    rng = np.random.default_rng(12)
+    n = 100_000
+    rel = _unit(rng, n)
+    dirs = -rel + 0.4 * _unit(rng, n)
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    wl = rng.uniform(300, 700, n)
+    for t, kind, model in (
+            (pp.make_generic_multipmt_om([1.0, 2.0, 3.0], 0.3, 4), "multipmt", None),
+            (pp.DOM.at([1.0, 2.0, 3.0], 5), "dom", None)):
+        pos = (np.array(t.shape.position) + t.shape.radius * rel).astype(np.float32)
+        got = pp.check_pmt_hit(pos, dirs, wl, t, seed=21)
+        m = dict(multipmt=_multipmt_dict(pp, t)) if kind == "multipmt" else \
+            dict(dom=_dom_dict(pp, None, apply_wl=False))
+        want, _ = pmt_oracle.detect(pos, wl.astype(np.float32), np.ones(n),
+                                    [dict(position=t.shape.position, radius=t.shape.radius,
+                                          kind=kind, active_area=t.pmt_area)], m, 21,
+                                    directions=dirs.astype(np.float32))
+        assert (got == want).mean() > 0.9999, kind
+        assert (got > 0).sum() > 500, kind
