@@ -275,3 +275,53 @@ def test_validation_formula(pp, gpu_ctx):
     assert 10.0 < L < 60.0, L
     assert 0.3 < norm < 3.0, norm
     assert np.max(np.abs(w / model - 1)) < 0.3, w / model
+
+
+def test_c1_full_size_properties(pp, orc, gpu_ctx):
+    """At the benchmark's size (C1, 1e8 photons): the hit set is bitwise the
+    same for two launch shapes, the union of four photon-range shards is
+    bitwise the single run, and the hit rate agrees with the oracle's on the
+    run's first 1.5e6 photons."""
+    import copy
+    setup = pp.workloads.c1_setup(photons=100_000_000, seed=1)
+    n = pp.source_photons(setup.sources[0].photons, setup.photon_scaling)
+    cap = 1_000_000
+
+    def sorted_cols(cols):
+        o = np.argsort(cols["photon_index"])
+        return {k: v[o] for k, v in cols.items()}
+    rc, base, nh, nsim = gpu_run(pp, setup, capacity=cap)
+    assert rc == 0 and nsim == n and nh > 5000
+    base = sorted_cols(base)
+    rc, other, _, _ = gpu_run(pp, setup, capacity=cap, block_threads=256, photons_per_thread=8,
+                              cell_size=25.0)
+    other = sorted_cols(other)
+    for k in base:
+        np.testing.assert_array_equal(other[k], base[k], err_msg=k)
+    parts = []
+    src = setup.sources[0]
+    for r in range(4):
+        lo, hi = n * r // 4, n * (r + 1) // 4
+        c = copy.copy(src)
+        c.photons, c.first_photon = hi - lo, lo
+        s = copy.copy(setup)
+        s.sources = [c]
+        rc, cols, _, sim = gpu_run(pp, s, capacity=cap)
+        assert rc == 0 and sim == hi - lo
+        parts.append(cols)
+    merged = sorted_cols({k: np.concatenate([p[k] for p in parts]) for k in base})
+    for k in base:
+        np.testing.assert_array_equal(merged[k], base[k], err_msg=k)
+    # the oracle on the first 1.5e6 photons of the same run
+    m = 1_500_000
+    c = copy.copy(src)
+    c.photons = m
+    s = copy.copy(setup)
+    s.sources = [c]
+    want, sim, _ = orc.Run.from_setup(s).propagate_all()
+    assert sim == m
+    first = {k: v[base["photon_index"] < m] for k, v in base.items()}
+    st = compare(first, oracle_columns(want), spheres_of(setup), mode="fast")
+    assert st["matched"] > 100, st
+    rate_all, rate_or = nh / n, len(want) / m
+    assert abs(rate_all - rate_or) < 5 * np.sqrt(rate_or / m), (rate_all, rate_or)
