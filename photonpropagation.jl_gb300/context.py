@@ -80,6 +80,7 @@ class Context:
         self.ptr = p
         self.device = device
         self._keep = {}
+        self.uploaded = None  # what the last PhotonPropSetup.upload sent
 
     def close(self):
         if getattr(self, "ptr", None) and self.ptr.value:
@@ -100,6 +101,7 @@ class Context:
 
     # -- tables -------------------------------------------------------------
     def set_medium(self, t) -> None:
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         arrs = [np.ascontiguousarray(a, np.float32) for a in
                 (t.scattering_length, t.group_velocity, t.absorption_length,
                  t.phase_refractive_index)]
@@ -115,29 +117,35 @@ class Context:
         check(self._lib.pp_set_medium(self.ptr, byref(m)), "pp_set_medium")
 
     def set_spectrum(self, knots) -> None:
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         k = np.ascontiguousarray(knots, np.float32)
         check(self._lib.pp_set_spectrum(self.ptr, k.ctypes.data_as(ctypes.POINTER(c_float)),
                                         k.shape[0]), "pp_set_spectrum")
 
     def set_monochromatic(self, wl: float) -> None:
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         check(self._lib.pp_set_monochromatic(self.ptr, float(wl)), "pp_set_monochromatic")
 
     def set_track_smear(self, q) -> None:
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         q = np.ascontiguousarray(q, np.float32)
         check(self._lib.pp_set_track_smear(self.ptr, q.ctypes.data_as(ctypes.POINTER(c_float)),
                                            q.shape[0]), "pp_set_track_smear")
 
     def set_track_smear_tables(self, q) -> None:
         """(n_tables, n_knots) quantile tables; a source uses its smear_table."""
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         q = np.ascontiguousarray(np.atleast_2d(q), np.float32)
         check(self._lib.pp_set_track_smear_tables(
             self.ptr, q.ctypes.data_as(ctypes.POINTER(c_float)), q.shape[1], q.shape[0]),
             "pp_set_track_smear_tables")
 
     def set_targets(self, spheres, n: int, cell_size: float = 0.0) -> None:
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         check(self._lib.pp_set_targets(self.ptr, spheres, n, float(cell_size)), "pp_set_targets")
 
     def set_shaped_targets(self, records, n: int) -> None:
+        self.uploaded = None  # device inputs changed outside PhotonPropSetup.upload
         check(self._lib.pp_set_shaped_targets(self.ptr, records, n), "pp_set_shaped_targets")
 
     def set_sources(self, records, n: int, scaling: float = 1.0) -> None:

@@ -6,7 +6,6 @@ import numpy as np
 
 from . import _lib
 from .context import Context, device_memory
-from . import targets as _targets
 from .targets import module_ids
 
 _CONTEXTS: dict = {}
@@ -54,11 +53,11 @@ def get_context(device: int = 0) -> Context:
 
 
 def _ensure_uploaded(setup, ctx) -> None:
-    key = (id(ctx), id(setup.medium), id(setup.spec_dist), _targets.identity(setup.targets),
-           setup.needs_track_smear())
-    if getattr(setup, "_uploaded_key", None) != key:
+    """Upload the setup's device inputs unless the context already holds them
+    (the context records what its last PhotonPropSetup.upload sent; any other
+    setter clears the record)."""
+    if not setup.is_uploaded(ctx):
         setup.upload(ctx)
-        setup._uploaded_key = key
 
 
 def _run(setup, hit_buffers: HitBuffers, n_steps: int):

@@ -126,3 +126,31 @@ class PhotonPropSetup:
             ctx.set_shaped_targets(self.target_records(), self.n_target_records())
         else:
             ctx.set_targets(self.sphere_records(), len(self.targets), cell_size)
+        ctx.uploaded = self.upload_signature(cell_size)
+
+    def upload_signature(self, cell_size: float = 0.0):
+        """What `upload` sent: the medium, spectrum and target objects themselves
+        (held, so compared by identity without id reuse) and the derived tables
+        by value.  Media, spectra and targets are taken as immutable once
+        uploaded, as the reference's structs are."""
+        targets = self.targets if isinstance(self.targets, _targets.DetectorLines) \
+            else tuple(self.targets)
+        tables = self.track_table_stack() if self.needs_track_smear() else None
+        return (self.medium, self.spec_dist, targets, self.spectrum_knots, self.mono_wavelength,
+                tables, float(cell_size))
+
+    def is_uploaded(self, ctx, cell_size: float = 0.0) -> bool:
+        """True when `ctx` holds exactly what `upload` would send."""
+        cur = getattr(ctx, "uploaded", None)
+        if cur is None:
+            return False
+        new = self.upload_signature(cell_size)
+        same_obj = cur[0] is new[0] and cur[1] is new[1] and (
+            cur[2] is new[2] or (isinstance(cur[2], tuple) and isinstance(new[2], tuple) and
+                                 len(cur[2]) == len(new[2]) and
+                                 all(a is b for a, b in zip(cur[2], new[2]))))
+        def eq(a, b):
+            return (a is None and b is None) or (a is not None and b is not None and
+                                                 np.array_equal(a, b))
+        return same_obj and eq(cur[3], new[3]) and cur[4] == new[4] and eq(cur[5], new[5]) \
+            and cur[6] == new[6]

@@ -79,13 +79,6 @@ def record_count(targets) -> int:
     return len(targets)
 
 
-def identity(targets) -> tuple:
-    """Key of a target list for upload caching."""
-    if isinstance(targets, DetectorLines):
-        return (id(targets),) + tuple(id(t) for line in targets.lines for t in line.targets)
-    return tuple(id(t) for t in targets)
-
-
 def to_spheres(targets) -> "_lib.pp_sphere array":
     arr = (_lib.pp_sphere * max(1, len(targets)))()
     for i, t in enumerate(targets):

@@ -203,3 +203,30 @@ def test_workload_shapes(pp):
     assert len(n) == 256 and n.min() >= 1e4 and n.max() <= 1e7
     kinds = [s.kind for s in s2.sources]
     assert kinds.count(0) == 128 and kinds.count(1) == 128
+
+
+def test_upload_record_follows_the_context(pp):
+    """The device inputs a context holds are recorded on the context: a setup
+    that another setup's upload replaced is uploaded again, equal derived
+    tables count as the same, and a low-level setter clears the record."""
+    import types
+    m = pp.CascadiaMediumProperties()
+    t = [pp.HomogeneousDetector(pp.Spherical([0.0, 0.0, 10.0], 0.3), 1.0, 1)]
+    lp = pp.LongitudinalParameterisation(2.0, 0.63, 0.36)
+    a = pp.PhotonPropSetup([pp.ExtendedCherenkovEmitter([0, 0, 0], [0, 0, 1.0], 0.0, 10, lp)], t,
+                           m, pp.make_monochromatic_spectrum(450.0), 1)
+    b = pp.PhotonPropSetup([pp.ExtendedCherenkovEmitterCustomSmear([0, 0, 0], [0, 0, 1.0], 0.0, 10,
+                                                                   lp, 2.0, 0.5)], t, m,
+                           pp.make_monochromatic_spectrum(450.0), 1)
+    ctx = types.SimpleNamespace(uploaded=None)
+    assert not a.is_uploaded(ctx)
+    ctx.uploaded = a.upload_signature()
+    assert a.is_uploaded(ctx)
+    # same medium and targets, but another spectrum object and other smear tables
+    assert not b.is_uploaded(ctx)
+    ctx.uploaded = b.upload_signature()
+    assert not a.is_uploaded(ctx)  # b's upload replaced a's inputs
+    c = pp.PhotonPropSetup(list(a.sources), list(t), m, a.spec_dist, 2)
+    ctx.uploaded = a.upload_signature()
+    assert c.is_uploaded(ctx)  # same objects, another seed: nothing to send
+    assert not a.is_uploaded(types.SimpleNamespace(uploaded=None))

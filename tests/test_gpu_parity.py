@@ -20,7 +20,6 @@ def gpu_run(pp, setup, n_steps=15, capacity=None, **tuning):
         if tuning:
             ctx.set_tuning(**tuning)
         setup.upload(ctx)
-        setup._uploaded_key = None
         recs = setup.source_records()
         cap = capacity if capacity is not None else sum(
             pp.source_photons(s.photons, setup.photon_scaling) for s in setup.sources)
@@ -212,7 +211,6 @@ def test_graph_launch_matches_plain_launch(pp, gpu_ctx):
     setup = pp.workloads.c1_setup(photons=500_000, seed=4)
     ctx = pp.get_context(0)
     setup.upload(ctx)
-    setup._uploaded_key = None
     recs = setup.source_records()
     ctx.set_sources(recs, len(setup.sources), 1.0)
     cap = 500_000
@@ -240,7 +238,6 @@ def test_photon_steps_counter(pp, orc, gpu_ctx):
     setup = pp.workloads.c0_setup(100_000)
     ctx = pp.get_context(0)
     setup.upload(ctx)
-    setup._uploaded_key = None
     ctx.set_sources(setup.source_records(), 1, 1.0)
     hits = torch.zeros(100_000 * 20, dtype=torch.int32, device="cuda")
     ctr = torch.zeros(12, dtype=torch.int32, device="cuda")

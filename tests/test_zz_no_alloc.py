@@ -80,7 +80,6 @@ def test_static_scratch_matches_context_entry_point(pp, gpu_ctx, which):
     # existing entry point (context-owned buffers)
     ctx = pp.get_context(0)
     setup.upload(ctx)
-    setup._uploaded_key = None
     rc, n_ref, sim_ref = ctx.propagate(setup.source_records(), len(setup.sources), setup.seed, 15,
                                        setup.photon_scaling, capacity)
     assert rc == 0 and n_ref > 10
