@@ -36,4 +36,16 @@ from .generic_multipmt import (SphericalMultiPMTTarget, fibonacci_sphere,
 from .detection import (InterpQuantumEff, apply_qe, apply_wl_acceptance, calc_pe_weight,
                         check_pmt_hit, check_pmt_hit_opening_angle, make_hits_from_photons)
 
+from .calc import (calc_time_residual_cascades, calc_time_residual_tracks, shift_particle,
+                   shift_to_closest_approach)
+from .particles import (AngularEmissionProfile, CherenkovTrackLengthParameters,
+                        FastLightsabreMuonEmitter, LongitudinalParametersBase,
+                        cherenkov_ang_dist, cherenkov_ang_dist_int, get_longitudinal_params)
+from .pom import POMAcceptance, POMRelativeAcceptance, get_pom_pmt_group
+from .processing import PhotonHit
+from .sources import _CherenkovBase as CherenkovEmitter
+from .spectrum import make_cuda_spectral_dist
+from .targets import check_intersection
+
 __all__ = [n for n in dir() if not n.startswith("_")]
+

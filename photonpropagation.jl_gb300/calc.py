@@ -56,6 +56,21 @@ def calc_tgeo_tracks(p0, direction, pos, medium_or_n_ph, n_grp=None, wavelength=
     return (along + dist * (n_grp * n_ph - 1.0) / np.sqrt(n_ph ** 2 - 1.0)) / C_VAC_M_NS
 
 
+def shift_particle(particle, param):
+    """The particle moved by `param` m along its direction, its time by
+    param / c (src/calc.jl:236-247)."""
+    from dataclasses import replace
+    pos = np.asarray(particle.position, np.float64) + param * np.asarray(particle.direction,
+                                                                         np.float64)
+    return replace(particle, position=list(pos), time=particle.time + param / C_VAC_M_NS)
+
+
+def shift_to_closest_approach(particle, pos):
+    """The particle shifted to its closest approach to `pos` (src/calc.jl:249-265)."""
+    return shift_particle(particle, float(closest_approach_param(particle.position,
+                                                                 particle.direction, pos)))
+
+
 def module_tgeo(setup) -> np.ndarray:
     """Geometric time of every target for the setup's first source, as
     calc_time_residual! uses it (src/calc.jl:270-323)."""
@@ -69,6 +84,33 @@ def module_tgeo(setup) -> np.ndarray:
             dist = np.linalg.norm(np.asarray(src.position, np.float64) - pos)
             out[i] = calc_tgeo(dist, setup.medium, target=t)
     return out
+
+
+def _residuals(table, setup, tg):
+    index_of = {int(getattr(t, "module_id", i + 1)): i for i, t in enumerate(setup.targets)}
+    rows = np.array([index_of[int(m)] for m in table["module_id"]], np.int64) \
+        if len(table["module_id"]) else np.zeros(0, np.int64)
+    table["tres"] = np.asarray(table["time"], np.float64) - tg[rows] - float(setup.sources[0].time)
+    return table
+
+
+def calc_time_residual_tracks(table, setup):
+    """``calc_time_residual_tracks!`` (src/calc.jl:283-298): the track form for
+    every module, the first source taken as the track."""
+    src = setup.sources[0]
+    tg = np.array([calc_tgeo_tracks(src.position, src.direction,
+                                    np.asarray(t.shape.position, np.float64), setup.medium)
+                   for t in setup.targets], np.float64)
+    return _residuals(table, setup, tg)
+
+
+def calc_time_residual_cascades(table, setup):
+    """``calc_time_residual_cascades!`` (src/calc.jl:301-312)."""
+    src = setup.sources[0]
+    tg = np.array([calc_tgeo(np.linalg.norm(np.asarray(src.position, np.float64) -
+                                            np.asarray(t.shape.position, np.float64)),
+                             setup.medium, target=t) for t in setup.targets], np.float64)
+    return _residuals(table, setup, tg)
 
 
 def calc_time_residual(table, setup):

@@ -45,6 +45,38 @@ def particle_shape(p: Particle) -> str:
     raise ValueError(f"unknown particle type {p.type}")
 
 
+@dataclass(frozen=True)
+class LongitudinalParametersBase:
+    """Longitudinal profile parameters at 1 GeV (src/lightyield.jl:133-158)."""
+    alpha: float
+    beta: float
+    b: float
+
+
+def get_longitudinal_params(ptype: str, energy: float | None = None):
+    """The type's LongitudinalParametersBase, or with `energy` (GeV) the
+    energy-corrected (a, b) = (alpha + beta log10 E, b) (src/lightyield.jl:155-172)."""
+    from .sources import LONGITUDINAL_PARAMETERS
+    base = LongitudinalParametersBase(*LONGITUDINAL_PARAMETERS[ptype])
+    if energy is None:
+        return base
+    return base.alpha + base.beta * math.log10(energy), base.b
+
+
+@dataclass(frozen=True)
+class CherenkovTrackLengthParameters:
+    """alpha E^beta (and its spread alpha_dev E^beta_dev) of the Cherenkov track
+    length (src/lightyield.jl:200-238)."""
+    alpha: float
+    beta: float
+    alpha_dev: float
+    beta_dev: float
+
+
+class AngularEmissionProfile:
+    """Marker type of the reference (src/lightyield.jl:39), no fields."""
+
+
 # Cherenkov track length parametrisation, src/lightyield.jl:212-238
 # (alpha, beta, alpha_dev, beta_dev) per particle type.
 TRACK_LENGTH_PARAMETERS = {
@@ -123,8 +155,49 @@ def cherenkov_ang_dist(costheta, ref_index, pars=STD_ANG_DIST_PARS):
     return a * np.exp(b * np.abs(np.asarray(costheta, np.float64) - 1.0 / ref_index) ** c) + d
 
 
-def cherenkov_ang_dist_int(ref_index, lower=-1.0, upper=1.0, pars=STD_ANG_DIST_PARS):
-    """Integral of cherenkov_ang_dist over [lower, upper].  On each side of the
+def cherenkov_ang_dist_int_analytic(ref_index, lower=-1.0, upper=1.0, pars=STD_ANG_DIST_PARS):
+    """The reference's closed form of the integral (src/lightyield.jl:73-111):
+    on each side of the peak cos(theta_c) = 1/n the antiderivative
+    (c d x + a (cc - x) Gamma(1/c, -b |x - cc|^c) (-b |x - cc|^c)^(-1/c)) / c
+    with the upper incomplete gamma function, the upper branch shifted by twice
+    the lower branch's value just below the peak.  That shift includes the
+    d x term, so across the peak the result differs from the true integral by
+    about 2 d cos(theta_c) (-0.0015 at n = 1.34); reproduced as the reference
+    computes it (cherenkov_ang_dist_int_quad gives the true integral)."""
+    a, b, c, d = pars
+    cc = 1.0 / ref_index
+
+    def branch(x, z):
+        zz = -b * z ** c
+        return (c * d * x + a * (cc - x) * special.gammaincc(1 / c, zz) * special.gamma(1 / c)
+                * zz ** (-1 / c)) / c
+
+    peak = branch(cc - 1e-5, 1e-5)
+
+    def indef(x):
+        return branch(x, cc - x) if x <= cc else branch(x, x - cc) + 2 * peak
+
+    return indef(upper) - indef(lower)
+
+
+# cherenkov_ang_dist_int(ref_index): the reference's linear interpolation of the
+# closed form over [-1, 1] on n = 1.1:0.01:1.5 (src/lightyield.jl:113-130)
+_ANG_INT_N = np.round(np.arange(1.1, 1.5 + 1e-9, 0.01), 10)
+_ANG_INT_A = np.array([cherenkov_ang_dist_int_analytic(n) for n in _ANG_INT_N])
+
+
+def cherenkov_ang_dist_int(ref_index):
+    """Integral of cherenkov_ang_dist over [-1, 1] at `ref_index` in [1.1, 1.5],
+    interpolated linearly as the reference's ChAngDistInt does."""
+    r = np.asarray(ref_index, np.float64)
+    if np.any((r < _ANG_INT_N[0] - 1e-12) | (r > _ANG_INT_N[-1] + 1e-12)):
+        raise ValueError("refractive index outside the interpolation range [1.1, 1.5]")
+    return np.interp(r, _ANG_INT_N, _ANG_INT_A)
+
+
+def cherenkov_ang_dist_int_quad(ref_index, lower=-1.0, upper=1.0, pars=STD_ANG_DIST_PARS):
+    """Integral of cherenkov_ang_dist over [lower, upper] by quadrature (an
+    independent check of the closed form).  On each side of the
     peak cos(theta_c) = 1/n the substitution s = |x - 1/n|^c turns the cusp
     into the smooth integrand (a e^(b s) + d) s^(1/c - 1) / c, integrated by
     Gauss-Legendre quadrature."""
@@ -200,6 +273,9 @@ def fast_lightsabre_muon_emitter(particle, medium, spectrum, rng=None):
     n = _poisson(total_lightyield(particle, medium, spectrum) + ly_stoch, rng)
     return CherenkovTrackEmitter(list(particle.position), list(particle.direction),
                                  particle.time, particle.length, n)
+
+
+FastLightsabreMuonEmitter = fast_lightsabre_muon_emitter  # the reference's constructor name
 
 
 def split_source(source, parts: int):

@@ -123,3 +123,22 @@ def pom_model(orientation=None, tables: POMTables | None = None) -> "_lib.pp_pom
             m.pmt_dir[i][k] = float(d[i, k])
         m.pmt_group[i] = int(POM_PMT_GROUP[i])
     return m
+
+
+POMAcceptance = POMTables  # the reference's name for the acceptance model (src/pom.jl:16-33)
+
+
+class POMRelativeAcceptance:
+    """The reference's relative-acceptance POM model (src/pom.jl:44-60), whose
+    check_pmt_hit raises "Not Implemented" (src/pom.jl:190-197): detection
+    with it raises here too."""
+
+    def __init__(self, *args, **kwargs):
+        raise NotImplementedError("POMRelativeAcceptance: check_pmt_hit is not implemented "
+                                  "in the reference either")
+
+
+def get_pom_pmt_group(pmt_ix: int) -> int:
+    """Group (1 or 2) of the 1-based PMT index (src/pom.jl:160-162)."""
+    return int(POM_PMT_GROUP[int(pmt_ix) - 1])
+

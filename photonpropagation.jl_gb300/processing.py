@@ -2,6 +2,8 @@
 src/photon_prop_cuda.jl:878-959)."""
 from __future__ import annotations
 
+from dataclasses import dataclass
+
 import numpy as np
 
 from . import _lib
@@ -15,6 +17,20 @@ class PhotonPropOOMException(Exception):
     """The hit buffer was too small (src/photon_prop_cuda.jl:40, :937-939)."""
 
 
+@dataclass
+class PhotonHit:
+    """One row of the hit table (PhotonHit, src/photon_prop_cuda.jl:407-416),
+    for code that walks hits one by one; ``HitTable.rows()`` yields them."""
+    position: np.ndarray
+    direction: np.ndarray
+    initial_direction: np.ndarray
+    wavelength: float
+    time: float
+    dist_travelled: float
+    module_id: int
+    n_steps: int
+
+
 class HitTable(dict):
     """Column table of hits (the reference returns a DataFrame with these
     columns; numpy arrays keyed by column name here)."""
@@ -22,6 +38,13 @@ class HitTable(dict):
     @property
     def nrow(self) -> int:
         return int(self["wavelength"].shape[0]) if "wavelength" in self else 0
+
+    def rows(self):
+        for i in range(self.nrow):
+            yield PhotonHit(self["position"][i], self["direction"][i],
+                            self["initial_direction"][i], float(self["wavelength"][i]),
+                            float(self["time"][i]), float(self["dist_travelled"][i]),
+                            int(self["module_id"][i]), int(self["n_steps"][i]))
 
 
 class HitBuffers:

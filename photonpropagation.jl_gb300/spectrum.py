@@ -100,6 +100,15 @@ def make_cherenkov_spectrum(wl_range, medium) -> Spectrum:
                     (float(wl_range[0]), float(wl_range[1])))
 
 
+def make_cuda_spectral_dist(spec: SpectralDist, wl_range=None, interp_steps: int = 30):
+    """``make_cuda_spectral_dist(spec, wl_range, interp_steps)`` (src/spectrum.jl:75-83):
+    the inverse CDF sampled at `interp_steps` points of [0, 1] that the device
+    interpolates (PhotonPropSetup uses 600); a Monochromatic passes through."""
+    if isinstance(spec, Monochromatic):
+        return spec
+    return spec.device_knots(interp_steps)
+
+
 def make_biased_cherenkov_spectrum(bias_function: Callable, wl_range, medium) -> Spectrum:
     """Frank-Tamm spectrum times `bias_function(wl)` (e.g. a module's wavelength
     acceptance), its CDF tabulated every 0.5 nm (src/spectrum.jl:97-101)."""

@@ -145,3 +145,35 @@ def module_ids(targets) -> np.ndarray:
                         "kernel's module index t + N * line")
     return np.asarray([int(getattr(t, "module_id", i + 1)) for i, t in enumerate(targets)],
                       np.uint16)
+
+
+def check_intersection(shape, pos, direction, step):
+    """``check_intersection(shape, pos, dir, step)`` (src/photon_prop_cuda.jl:309-404),
+    host form in FP32 as the device evaluates it: (hit, distance) for a sphere
+    (the near root strictly inside (0, step)), a horizontal rectangle or a
+    disc (met at d = (z_s - z) / dir_z in [0, step], strictly inside)."""
+    f = np.float32
+    p = np.asarray(pos, f)
+    d = np.asarray(direction, f)
+    L = f(step)
+    c = np.asarray(shape.position, f)
+    if isinstance(shape, Spherical):
+        dp = (p - c).astype(f)
+        a = f(np.dot(d, dp))
+        b = f(a * a - (f(np.dot(dp, dp)) - f(shape.radius) * f(shape.radius)))
+        dist = f(-a - np.sqrt(abs(b))) if b >= 0 else f(-1)
+        return (True, float(dist)) if (dist > 0 and dist < L) else (False, float("nan"))
+    if d[2] == 0:
+        return False, float("nan")
+    dist = f((c[2] - p[2]) / d[2])
+    if dist < 0 or dist > L:
+        return False, float("nan")
+    x, y = f(p[0] + d[0] * dist - c[0]), f(p[1] + d[1] * dist - c[1])
+    if isinstance(shape, Rectangular):
+        inside = abs(x) < f(0.5) * f(shape.length_x) and abs(y) < f(0.5) * f(shape.length_y)
+    elif isinstance(shape, Circular):
+        inside = x * x + y * y < f(shape.radius) * f(shape.radius)
+    else:
+        raise TypeError(f"no intersection test for {type(shape).__name__}")
+    return (True, float(dist)) if inside else (False, float("nan"))
+

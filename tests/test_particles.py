@@ -49,7 +49,29 @@ def test_longitudinal_profile_and_angular_distribution(pp, medium_spectrum):
         np.trapezoid(P.longitudinal_profile(z[1:20001], lp), z[1:20001] / lp.lrad), abs=1e-4)
     x = np.linspace(-1, 1, 2_000_001)
     dense = np.trapezoid(P.cherenkov_ang_dist(x, 1.34), x)
-    assert P.cherenkov_ang_dist_int(1.34) == pytest.approx(dense, rel=1e-5)
+    assert P.cherenkov_ang_dist_int_quad(1.34) == pytest.approx(dense, rel=1e-5)
+    # the reference's closed form: exact away from the peak; across it, off by
+    # 2 (L(cc - 1e-5) - K), L the lower branch and K = a Gamma(1/c) (-b)^(-1/c) / c
+    from scipy import special
+    a, b, c, d = P.STD_ANG_DIST_PARS
+    for n in (1.1, 1.3, 1.34, 1.5):
+        cc = 1 / n
+        assert P.cherenkov_ang_dist_int_analytic(n, 0.2, 0.6 if n > 1.3 else 0.55) == \
+            pytest.approx(P.cherenkov_ang_dist_int_quad(n, 0.2, 0.6 if n > 1.3 else 0.55),
+                          rel=1e-9)
+        zz = -b * 1e-5 ** c
+        L = d * (cc - 1e-5) + a * 1e-5 * special.gammaincc(1 / c, zz) * special.gamma(1 / c) \
+            * zz ** (-1 / c) / c
+        K = a * special.gamma(1 / c) * (-b) ** (-1 / c) / c
+        assert P.cherenkov_ang_dist_int_analytic(n) - P.cherenkov_ang_dist_int_quad(n) == \
+            pytest.approx(2 * (L - K), abs=1e-9)
+    # the exported function interpolates the closed form on n = 1.1:0.01:1.5
+    assert P.cherenkov_ang_dist_int(1.34) == pytest.approx(
+        P.cherenkov_ang_dist_int_analytic(1.34), rel=1e-12)
+    mid = 0.5 * (P.cherenkov_ang_dist_int_analytic(1.34) + P.cherenkov_ang_dist_int_analytic(1.35))
+    assert P.cherenkov_ang_dist_int(1.345) == pytest.approx(mid, rel=1e-12)
+    with pytest.raises(ValueError):
+        P.cherenkov_ang_dist_int(1.6)
 
 
 def test_emitters_from_particles(pp, medium_spectrum):
