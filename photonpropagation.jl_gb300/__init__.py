@@ -46,6 +46,9 @@ from .processing import PhotonHit
 from .sources import _CherenkovBase as CherenkovEmitter
 from .spectrum import make_cuda_spectral_dist
 from .targets import check_intersection
+from . import output
+from .output import (dataframe_to_hit_list, event_info_to_dataframe, hit_list_to_dataframe,
+                     read_event, save_event, source_to_namedtuple, targets_to_dataframe)
 
 __all__ = [n for n in dir() if not n.startswith("_")]
 

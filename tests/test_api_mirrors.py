@@ -92,3 +92,33 @@ def test_spectrum_pom_and_hit_rows(pp):
     rows = list(t.rows())
     assert len(rows) == 2 and isinstance(rows[1], pp.PhotonHit)
     assert (rows[1].wavelength, rows[1].module_id, rows[1].n_steps) == (500.0, 6, 2)
+
+
+def test_output_tables_and_events(pp, tmp_path):
+    """Hit lists <-> hit tables round trip (with PMT noise added), module and
+    source tables, and save_event / read_event."""
+    rng = np.random.default_rng(3)
+    targets = [pp.POM.at([0.0, 0.0, 0.0], 4), pp.POM.at([0.0, 0.0, 20.0], 9)]
+    hits = [np.sort(rng.uniform(0, 100, rng.integers(0, 4))) for _ in range(32)]
+    pp.add_pmt_noise(hits, targets, noise_rate=1e5, time_window=1e3, rng=rng)
+    table = pp.hit_list_to_dataframe(hits, targets)
+    assert len(table["time"]) == sum(len(h) for h in hits)
+    back = pp.dataframe_to_hit_list(table, targets)
+    for a, b in zip(back, hits):
+        np.testing.assert_array_equal(np.sort(a), np.sort(b))
+    assert set(np.unique(table["module_id"])) <= {4, 9} and table["pmt_id"].max() <= 16
+    # only the second module (target_mask)
+    part = pp.hit_list_to_dataframe(hits[16:], targets, [False, True])
+    assert set(np.unique(part["module_id"])) <= {9}
+    mods = pp.targets_to_dataframe(targets)
+    assert len(mods["pmt_id"]) == 32 and mods["module_z"][-1] == 20.0
+    P = pp.particles
+    p = P.Particle([1.0, 2.0, 3.0], [0.0, 0.0, 1.0], 4.0, 1e3, 0.0, "EMinus")
+    info = pp.event_info_to_dataframe(p)
+    assert info["energy"][0] == 1e3 and info["z"][0] == 3.0
+    lp = pp.LongitudinalParameterisation(2.0, 0.63, 0.36)
+    srcs = [pp.ExtendedCherenkovEmitter([1.0, 2.0, 3.0], [0.0, 0.0, 1.0], 4.0, 1234, lp)]
+    pp.save_event(str(tmp_path), dict(event_id=7, hits=table, sources=srcs))
+    ev = pp.read_event(str(tmp_path), 7)
+    np.testing.assert_array_equal(ev["hits"]["time"], table["time"])
+    assert ev["sources"]["ExtendedCherenkovEmitter"]["n_photons"][0] == 1234
