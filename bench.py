@@ -82,6 +82,15 @@ def dist_env():
     return rank, world, local
 
 
+def workload_name(config: str) -> str:
+    """The workload both arms report in `config.workload`."""
+    if config == "c1":
+        return ("C1: 400 spheres r=0.2159 m on 20 strings (x,y ~ U(-250,250), "
+                "z=-250..225 step 25), isotropic point in the hull, 1e8 photons, "
+                "Frank-Tamm 300-800 nm, Cascadia water, 15 steps, seeds 1-5")
+    return "C0: README single-module example"
+
+
 def make_setups(pp, config, photons, n_seeds=5):
     if config == "c0":
         out = [pp.workloads.c0_setup(photons, seed=s) for s in range(1, n_seeds + 1)]
@@ -232,8 +241,9 @@ def run_reference(args):
         "unit": "photons/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.config.upper()}: reference algorithm (CPU oracle port; "
-                               "PhotonPropagation.jl/CUDA.jl is not runnable on this box)",
+        "config": {"workload": workload_name(args.config),
+                   "implementation": "the reference algorithm on the host cores (CPU oracle port; "
+                                     "PhotonPropagation.jl/CUDA.jl is not runnable on this box)",
                    "photons_per_step_sample": per_step, "photons_full": photons},
         "cpu_baseline": {"value": value, "unit": "photons/s", "cores": nthreads, "kind": "port",
                          "sample": f"{per_step} photons per step, {args.steps} steps"},
@@ -625,10 +635,7 @@ def run_ours(args):
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {
-            "workload": ("C1: 400 spheres r=0.2159 m on 20 strings (x,y ~ U(-250,250), "
-                         "z=-250..225 step 25), isotropic point in the hull, 1e8 photons, "
-                         "Frank-Tamm 300-800 nm, Cascadia water, 15 steps, seeds 1-5")
-            if args.config == "c1" else "C0: README single-module example",
+            "workload": workload_name(args.config),
             "photons_per_step": photons, "seeds": [1, 2, 3, 4, 5],
             "l2": "flushed between steps (512 MiB write)",
             "tuning": {"block_threads": tun.block_threads,
