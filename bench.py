@@ -345,6 +345,14 @@ def bench_surrogate(pp, torch, local, args):
     e1.record()
     torch.cuda.synchronize()
     step_ms = e0.elapsed_time(e1) / 20
+    # the same step as captured replays (batch drawn on the device included)
+    xp = [t.data_ptr() for t in (x, c, h)]
+    mlp.train_steps(*xp, n3, 8192, 3, 0, 10**9, 1e-6, 1e-6, 5, stream=cur)
+    e0.record()
+    mlp.train_steps(*xp, n3, 8192, 20, 0, 10**9, 1e-6, 1e-6, 5, stream=cur)
+    e1.record()
+    torch.cuda.synchronize()
+    graph_step_ms = e0.elapsed_time(e1) / 20
     flops_row = 2 * sum(r * cc for r, cc in
                         (mlp.layout(l)[2:] for l in range(mlp.n_layers + 1)))
     # C4
@@ -397,6 +405,8 @@ def bench_surrogate(pp, torch, local, args):
             "train_steps": args.c3_steps, "batch": 8192, "lr": 1e-3,
             "train_seconds": t_train, "train_step_ms": step_ms,
             "train_tflops": 3 * flops_row * 8192 / (step_ms * 1e-3) / 1e12,
+            "train_step_graph_ms": graph_step_ms,
+            "train_tflops_graph": 3 * flops_row * 8192 / (graph_step_ms * 1e-3) / 1e12,
             "loss_first": log[0][1], "loss_last": log[-1][1]},
         "c4_inference": {
             "workload": f"{n4} pairs from the training distributions; 1% audited by the MC "

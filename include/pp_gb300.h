@@ -392,6 +392,22 @@ PP_API int pp_mlp_loss_grad(pp_mlp* mlp, const float* d_x, const float* d_count,
 /* One Adam step (forward, backward, update), asynchronous on `stream`. */
 PP_API int pp_mlp_train_step(pp_mlp* mlp, const float* d_x, const float* d_count,
                              const float* d_hist, int32_t B, float lr, void* stream);
+/* n_steps Adam steps run by the library: each draws a batch of B rows
+ * uniformly, with replacement, from the n_rows training rows in device memory
+ * (d_x n_rows x n_in, d_count n_rows, d_hist n_rows x n_bins; row i of the
+ * batch of Adam step t is Philox4x32-10(i, t, tag; key = seed) scaled to
+ * n_rows), and takes a step of size lr1 + (lr0 - lr1) (1 + cos(pi s / (total - 1))) / 2,
+ * s = t - step0 the step's index in a cosine schedule that began at Adam step
+ * step0.  One step is captured once as a CUDA graph (for these arguments) and
+ * replayed, so n_steps calls cost n_steps graph launches; batches and step
+ * sizes depend only on the global step index, so K1 then K2 steps equal
+ * K1 + K2 steps in one call.  Asynchronous on `stream`. */
+PP_API int pp_mlp_train_steps(pp_mlp* mlp, const float* d_x, const float* d_count,
+                              const float* d_hist, int64_t n_rows, int32_t B, int32_t n_steps,
+                              int64_t step0, int64_t total, float lr0, float lr1, uint64_t seed,
+                              void* stream);
+/* Adam steps taken so far. */
+PP_API int pp_mlp_step_count(const pp_mlp* mlp, int64_t* steps);
 PP_API int pp_mlp_last_loss(pp_mlp* mlp, float* host_loss);
 /* Adam moments (n = pp_mlp_num_params floats each; NULL skips one on get)
  * and step count, for training checkpoints. */

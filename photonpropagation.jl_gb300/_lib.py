@@ -222,6 +222,10 @@ SIGNATURES = {
     "pp_mlp_forward": (c_int32, [c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
     "pp_mlp_loss_grad": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32,
                                    POINTER(c_float), POINTER(c_float), c_void_p]),
+    "pp_mlp_train_steps": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int32,
+                                     c_int32, c_int64, c_int64, c_float, c_float, c_uint64,
+                                     c_void_p]),
+    "pp_mlp_step_count": (c_int32, [c_void_p, POINTER(c_int64)]),
     "pp_mlp_train_step": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_float,
                                     c_void_p]),
     "pp_mlp_last_loss": (c_int32, [c_void_p, POINTER(c_float)]),

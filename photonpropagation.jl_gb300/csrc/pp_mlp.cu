@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "pp_device.cuh"
 #include "pp_internal.h"
 #include "pp_tc.cuh"
 
@@ -358,6 +359,62 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
   const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
   w[i] = wi;
   w16[i] = __float2bfloat16(wi);
+}
+
+// Adam with its step size and bias corrections read from device memory
+// (sched[0..2], written by schedule_kernel), for the captured training step.
+__global__ void adam_dev_kernel(float* __restrict__ w, const float* __restrict__ g,
+                                float* __restrict__ m, float* __restrict__ v, long long n,
+                                const float* __restrict__ sched, float b1, float b2, float eps,
+                                bf16* __restrict__ w16) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float lr = sched[0], bc1 = sched[1], bc2 = sched[2];
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.0f - b1) * gi;
+  const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  w[i] = wi;
+  w16[i] = __float2bfloat16(wi);
+}
+
+// The step about to be taken (Adam step t = *step + 1): its cosine step size
+// and bias corrections.
+__global__ void schedule_kernel(const long long* __restrict__ step, long long step0,
+                                long long total, float lr0, float lr1, float b1, float b2,
+                                float* __restrict__ sched) {
+  const long long done = *step;
+  const double frac = total > 1 ? (double)(done - step0) / (double)(total - 1) : 0.0;
+  sched[0] = (float)((double)lr1 + 0.5 * ((double)lr0 - (double)lr1) *
+                                       (1.0 + cos(3.14159265358979323846 * frac)));
+  sched[1] = 1.0f - powf(b1, (float)(done + 1));
+  sched[2] = 1.0f - powf(b2, (float)(done + 1));
+}
+
+__global__ void step_kernel(long long* step) { *step += 1; }
+__global__ void set_step_kernel(long long* step, long long v) { *step = v; }
+
+// Batch row i of Adam step t = *step + 1: training row
+// floor(Philox(i, t, tag) * n_rows / 2^64), one warp per batch row.
+constexpr uint32_t kBatchTag = 0x42415443u;  // Philox counter word of the batch stream
+__global__ void gather_kernel(const float* __restrict__ x, const float* __restrict__ c,
+                              const float* __restrict__ h, long long n_rows, int n_in,
+                              int n_bins, int B, const long long* __restrict__ step,
+                              uint32_t k0, uint32_t k1, float* __restrict__ bx,
+                              float* __restrict__ bc, float* __restrict__ bh) {
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= B) return;
+  const unsigned long long t = (unsigned long long)(*step + 1);
+  const uint4 r = ppdev::philox(make_uint4((uint32_t)i, (uint32_t)t, (uint32_t)(t >> 32), kBatchTag),
+                                k0, k1);
+  const unsigned long long u = ((unsigned long long)r.x << 32) | r.y;
+  const long long row = (long long)__umul64hi(u, (unsigned long long)n_rows);
+  for (int j = lane; j < n_in; j += 32) bx[(long long)i * n_in + j] = x[row * n_in + j];
+  for (int j = lane; j < n_bins; j += 32) bh[(long long)i * n_bins + j] = h[row * n_bins + j];
+  if (lane == 0) bc[i] = c[row];
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* __restrict__ y) {
@@ -838,7 +895,8 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 // Grid: 128-row tiles x 128-column tiles x K splits of at most 256.  The
 // split size must be a multiple of kKC (except when one split covers all of K).
-cudaError_t launch_gemm(const GemmParams& p, cudaStream_t s) {
+// The GEMM's shared-memory opt-in, once per process (before any capture).
+cudaError_t gemm_setup() {
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -846,6 +904,11 @@ cudaError_t launch_gemm(const GemmParams& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
+  return cudaSuccess;
+}
+
+cudaError_t launch_gemm(const GemmParams& p, cudaStream_t s) {
+  if (cudaError_t e = gemm_setup()) return e;
   const int splits = (p.K + p.k_per_split - 1) / p.k_per_split;
   const int stages = std::min(kGemmStages, (p.k_per_split + kKC - 1) / kKC);
   dim3 grid((p.M + kTileM - 1) / kTileM, (p.N + kTileN - 1) / kTileN, splits);
@@ -885,6 +948,24 @@ struct pp_mlp {
   size_t infer_smem = 0;
   long long step = 0;
   float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f, time_weight = 1.0f;
+  // pp_mlp_train_steps: batch buffers, device step counter and schedule
+  // scalars, and the captured step with the arguments it was captured for
+  float *bx = nullptr, *bc = nullptr, *bh = nullptr;
+  long long* d_step = nullptr;
+  float* d_sched = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t step_graph = nullptr;
+  struct GraphKey {
+    const float *x, *c, *h;
+    long long n_rows, step0, total;
+    int B;
+    float lr0, lr1;
+    unsigned long long seed;
+    bool operator==(const GraphKey& o) const {
+      return x == o.x && c == o.c && h == o.h && n_rows == o.n_rows && step0 == o.step0 &&
+             total == o.total && B == o.B && lr0 == o.lr0 && lr1 == o.lr1 && seed == o.seed;
+    }
+  } graph_key{};
 };
 
 namespace {
@@ -894,6 +975,9 @@ void mlp_free(pp_mlp* m) {
   cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16); cudaFree(m->dO32);
   cudaFree(m->dZ[0]); cudaFree(m->dZ[1]); cudaFree(m->loss); cudaFree(m->err);
   cudaFree(m->wpack);
+  cudaFree(m->bx); cudaFree(m->bc); cudaFree(m->bh); cudaFree(m->d_step); cudaFree(m->d_sched);
+  if (m->step_graph) cudaGraphExecDestroy(m->step_graph);
+  if (m->cap_stream) cudaStreamDestroy(m->cap_stream);
   for (auto* p : m->Z) cudaFree(p);
   for (auto* p : m->Y) cudaFree(p);
 }
@@ -1232,8 +1316,89 @@ PP_API int pp_mlp_train_step(pp_mlp* m, const float* d_x, const float* d_count,
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "adam");
 }
 
+// Capture one training step (schedule, batch, forward, backward, Adam, step
+// count) on the library's own stream into m->step_graph.
+int capture_train_step(pp_mlp* m, const pp_mlp::GraphKey& k) {
+  if (m->step_graph) {
+    cudaGraphExecDestroy(m->step_graph);
+    m->step_graph = nullptr;
+  }
+  cudaError_t e = cudaSuccess;
+  if (!m->cap_stream) e = cudaStreamCreateWithFlags(&m->cap_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !m->bx) {
+    e = cudaMalloc(&m->bx, sizeof(float) * (size_t)m->max_batch * m->n_in);
+    if (e == cudaSuccess) e = cudaMalloc(&m->bc, sizeof(float) * (size_t)m->max_batch);
+    if (e == cudaSuccess) e = cudaMalloc(&m->bh, sizeof(float) * (size_t)m->max_batch * m->n_bins);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_step, sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_sched, sizeof(float) * 4);
+  }
+  if (e == cudaSuccess) e = gemm_setup();
+  if (e != cudaSuccess) return cuda_fail(e, "train-step setup");
+  cudaStream_t cs = m->cap_stream;
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+  schedule_kernel<<<1, 1, 0, cs>>>(m->d_step, k.step0, k.total, k.lr0, k.lr1, m->b1, m->b2,
+                                   m->d_sched);
+  gather_kernel<<<(unsigned)((k.B + 7) / 8), 256, 0, cs>>>(
+      k.x, k.c, k.h, k.n_rows, m->n_in, m->n_bins, k.B, m->d_step, (uint32_t)k.seed,
+      (uint32_t)(k.seed >> 32), m->bx, m->bc, m->bh);
+  int rc = mlp_forward(m, m->bx, k.B, cs);
+  if (rc == PP_OK) rc = mlp_backward(m, m->bc, m->bh, k.B, cs);
+  if (rc == PP_OK) {
+    adam_dev_kernel<<<(unsigned)((m->n_params + 255) / 256), 256, 0, cs>>>(
+        m->P, m->G, m->Mo, m->Vo, m->n_params, m->d_sched, m->b1, m->b2, m->eps, m->P16);
+    step_kernel<<<1, 1, 0, cs>>>(m->d_step);
+  }
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(cs, &g);  // always end the capture
+  if (rc != PP_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return rc != PP_OK ? rc : cuda_fail(e, "end capture");
+  }
+  e = cudaGraphInstantiate(&m->step_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    m->step_graph = nullptr;
+    return cuda_fail(e, "instantiate train step");
+  }
+  m->graph_key = k;
+  return PP_OK;
+}
+
 // Adam state for checkpoints: first and second moments (n floats each, either
 // may be null) and the step count.
+PP_API int pp_mlp_train_steps(pp_mlp* m, const float* d_x, const float* d_count,
+                              const float* d_hist, int64_t n_rows, int32_t B, int32_t n_steps,
+                              int64_t step0, int64_t total, float lr0, float lr1, uint64_t seed,
+                              void* stream) {
+  if (!m || !d_x || !d_count || !d_hist || n_rows < 1 || B < 1 || B > m->max_batch ||
+      n_steps < 0 || total < 1 || step0 < 0 || !(lr0 >= 0.0f) || !(lr1 >= 0.0f))
+    return fail(PP_ERR_INVALID, "pp_mlp_train_steps: bad arguments");
+  if (n_steps == 0) return PP_OK;
+  cudaSetDevice(m->device);
+  const pp_mlp::GraphKey k{d_x, d_count, d_hist, (long long)n_rows, (long long)step0,
+                           (long long)total, (int)B, lr0, lr1, (unsigned long long)seed};
+  if (!m->step_graph || !(m->graph_key == k)) {
+    const int rc = capture_train_step(m, k);
+    if (rc != PP_OK) return rc;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  // the device counter continues from the host's count
+  set_step_kernel<<<1, 1, 0, s>>>(m->d_step, m->step);
+  cudaError_t e = cudaGetLastError();
+  for (int i = 0; e == cudaSuccess && i < n_steps; ++i) e = cudaGraphLaunch(m->step_graph, s);
+  if (e != cudaSuccess) return cuda_fail(e, "pp_mlp_train_steps");
+  m->step += n_steps;
+  m->pack_dirty = true;
+  return PP_OK;
+}
+
+PP_API int pp_mlp_step_count(const pp_mlp* m, int64_t* steps) {
+  if (!m || !steps) return fail(PP_ERR_INVALID, "null argument");
+  *steps = m->step;
+  return PP_OK;
+}
+
 PP_API int pp_mlp_get_adam(const pp_mlp* m, float* host_m, float* host_v, int64_t n,
                            int64_t* step) {
   if (!m || n != m->n_params) return fail(PP_ERR_INVALID, "bad moment buffers");

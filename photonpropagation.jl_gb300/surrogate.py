@@ -244,6 +244,24 @@ class MLP:
                                           c_void_p(hist_dev), B, float(lr), c_void_p(stream)),
               "pp_mlp_train_step")
 
+    def train_steps(self, x_dev, count_dev, hist_dev, n_rows, B, n_steps, step0, total, lr0,
+                    lr1, seed, stream=0):
+        """`n_steps` Adam steps inside the library (pp_mlp_train_steps): batches
+        of `B` rows drawn on the device from the `n_rows` training rows, cosine
+        step size from `lr0` to `lr1` over `total` steps begun at Adam step
+        `step0`, one captured step replayed per step."""
+        check(self._lib.pp_mlp_train_steps(self.ptr, c_void_p(x_dev), c_void_p(count_dev),
+                                           c_void_p(hist_dev), int(n_rows), int(B), int(n_steps),
+                                           int(step0), int(total), float(lr0), float(lr1),
+                                           int(seed) & (2**64 - 1), c_void_p(stream)),
+              "pp_mlp_train_steps")
+
+    def step_count(self) -> int:
+        """Adam steps taken so far."""
+        v = c_int64()
+        check(self._lib.pp_mlp_step_count(self.ptr, byref(v)), "pp_mlp_step_count")
+        return v.value
+
     def save(self, path: str) -> None:
         """Checkpoint: shape, parameters and Adam state in one .npz file."""
         m = np.empty(self.n_params, np.float32)
@@ -276,32 +294,30 @@ class MLP:
 
 
 def train(mlp: MLP, x, counts, hists, steps: int, batch: int = 8192, lr: float = 1e-3,
-          seed: int = 0, log_every: int = 0, lr_final: float | None = None):
+          seed: int = 0, log_every: int = 0, lr_final: float | None = None, stream: int = 0):
     """Adam on (features, expected hits, time histograms) held in device memory
-    (torch tensors); returns the list of (step, loss) logged.  The step size
-    starts at `lr` and follows a cosine down to `lr_final` (default lr / 100)
-    at the last step, so that the final parameters are not those of one noisy
-    step at full rate."""
-    import math
+    (torch tensors, float32, contiguous); returns the list of (step, loss)
+    logged every `log_every` steps and at the last.  The step size starts at
+    `lr` and follows a cosine down to `lr_final` (default lr / 100) at the last
+    step, so that the final parameters are not those of one noisy step at full
+    rate.  Batches are drawn on the device (Philox, keyed on `seed` and the Adam
+    step), and the steps between two log points run as replays of one captured
+    step, without a return to Python."""
     lr_final = lr * 0.01 if lr_final is None else lr_final
-    import torch
+    x, counts, hists = (t.contiguous().float() for t in (x, counts, hists))
     n = x.shape[0]
-    g = torch.Generator(device="cuda")
-    g.manual_seed(seed)
-    log = []
-    bx = torch.empty((batch, x.shape[1]), dtype=torch.float32, device="cuda")
-    bc = torch.empty((batch,), dtype=torch.float32, device="cuda")
-    bh = torch.empty((batch, hists.shape[1]), dtype=torch.float32, device="cuda")
-    for s in range(steps):
-        idx = torch.randint(0, n, (batch,), device="cuda", generator=g)
-        torch.index_select(x, 0, idx, out=bx)
-        torch.index_select(counts, 0, idx, out=bc)
-        torch.index_select(hists, 0, idx, out=bh)
-        frac = s / max(1, steps - 1)
-        rate = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * frac))
-        mlp.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), batch, rate)
-        if log_every and (s % log_every == 0 or s == steps - 1):
-            log.append((s, mlp.last_loss()))
+    step0 = mlp.step_count()
+    points = sorted({s for s in range(0, steps, log_every)} | {steps - 1}) if log_every \
+        else [steps - 1]
+    log, done = [], 0
+    for p in points:
+        if p < 0:
+            continue
+        mlp.train_steps(x.data_ptr(), counts.data_ptr(), hists.data_ptr(), n, batch, p + 1 - done,
+                        step0, steps, lr, lr_final, seed, stream)
+        done = p + 1
+        if log_every:
+            log.append((p, mlp.last_loss()))
     return log
 
 

@@ -9,6 +9,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import mlp_oracle  # noqa: E402
+import pmt_oracle  # noqa: E402
 
 
 def _tiny_net(rng, n_in=3, hidden=5, layers=2, n_bins=4):
@@ -185,3 +186,82 @@ def test_fused_inference_follows_training(pp, gpu_ctx):
     lam, _ = mlp_oracle.MLPOracle(W, b, 8, 64).predict(x)
     np.testing.assert_allclose(np.log(e1.cpu().numpy()), np.log(lam), atol=1e-2)
     mlp.close()
+
+
+def _batch_rows(seed, step, B, n_rows):
+    """Rows of the batch of Adam step `step` (1-based) that pp_mlp_train_steps
+    draws: Philox4x32-10 of (i, step lo, step hi, 'BATC') keyed on the seed,
+    (x << 32 | y) * n_rows / 2^64."""
+    i = np.arange(B, dtype=np.uint64)
+    r = pmt_oracle.philox4x32_10(i, np.full(B, step & 0xFFFFFFFF), np.full(B, step >> 32),
+                                 np.full(B, 0x42415443), seed & 0xFFFFFFFF, seed >> 32)
+    u = (r[0].astype(object) << 32) | r[1].astype(object)
+    return np.array([int(v) * n_rows >> 64 for v in u], np.int64)
+
+
+def _same_run(p, q, steps, lr):
+    """Two training runs that took the same batches and step sizes.  The bias
+    gradients (and, above 256 rows, the weight gradients) are summed with
+    float atomics, so runs differ by rounding: nearly every parameter agrees
+    to 1e-6, and none by more than the Adam steps could move it."""
+    d = np.abs(p - q)
+    return np.mean(d > 1e-6) < 0.01 and d.max() <= 2 * steps * lr
+
+
+@pytest.mark.gpu
+def test_train_steps_chunks_are_one_run(pp, gpu_ctx):
+    """K1 then K2 captured steps equal K1 + K2 steps in one call (up to the
+    rounding of atomic gradient sums), and the batch seed changes the run."""
+    torch = pytest.importorskip("torch")
+    B, n = 256, 3000
+    x, count, hist, dev = _make(pp, n, seed=7)
+    ptrs = [t.data_ptr() for t in dev]
+    nets = [pp.surrogate.MLP(max_batch=B, seed=8) for _ in range(3)]
+    a, b, c = nets
+    a.train_steps(*ptrs, n, B, 5, 0, 12, 1e-3, 1e-5, 99)
+    a.train_steps(*ptrs, n, B, 7, 0, 12, 1e-3, 1e-5, 99)
+    b.train_steps(*ptrs, n, B, 12, 0, 12, 1e-3, 1e-5, 99)
+    c.train_steps(*ptrs, n, B, 12, 0, 12, 1e-3, 1e-5, 100)
+    torch.cuda.synchronize()
+    assert a.step_count() == b.step_count() == 12
+    assert _same_run(a.params(), b.params(), 12, 1e-3)
+    assert a.last_loss() == pytest.approx(b.last_loss(), rel=1e-4)
+    assert np.mean(np.abs(a.params() - c.params()) > 1e-6) > 0.5
+    for m in nets:
+        m.close()
+
+
+@pytest.mark.gpu
+def test_train_steps_match_host_loop(pp, gpu_ctx):
+    """The captured steps take the same batches (Philox rows, recomputed here)
+    and cosine step sizes as a host loop of pp_mlp_train_step, continuing the
+    Adam step count of earlier single steps."""
+    torch = pytest.importorskip("torch")
+    B, n, steps, seed = 256, 2000, 9, 0x123456789
+    x, count, hist, dev = _make(pp, n, seed=9)
+    a = pp.surrogate.MLP(max_batch=B, seed=10)
+    b = pp.surrogate.MLP(max_batch=B, seed=10)
+    for m in (a, b):  # two single steps first: the schedule starts at Adam step 2
+        m.train_step(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), B, 1e-3)
+        m.train_step(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), B, 1e-3)
+    a.train_steps(*[t.data_ptr() for t in dev], n, B, steps, 2, steps, 2e-3, 1e-4, seed)
+    for s in range(steps):
+        rows = torch.tensor(_batch_rows(seed, 2 + s + 1, B, n), device="cuda")
+        bx, bc, bh = (torch.index_select(t, 0, rows).contiguous() for t in dev)
+        rate = 1e-4 + 0.5 * (2e-3 - 1e-4) * (1.0 + np.cos(np.pi * s / (steps - 1)))
+        b.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), B, rate)
+    torch.cuda.synchronize()
+    assert a.step_count() == b.step_count() == steps + 2
+    assert _same_run(a.params(), b.params(), steps + 2, 2e-3)
+    assert a.last_loss() == pytest.approx(b.last_loss(), rel=1e-4)
+    for m in (a, b):
+        m.close()
+
+
+def test_train_steps_argument_checks(pp):
+    import ctypes
+    lib = pp._lib.load()
+    z = ctypes.c_void_p(0)
+    assert lib.pp_mlp_train_steps(z, z, z, z, 10, 8, 1, 0, 1, 1e-3, 1e-5, 0, z) != 0
+    v = ctypes.c_int64()
+    assert lib.pp_mlp_step_count(z, ctypes.byref(v)) != 0
