@@ -1,5 +1,6 @@
 // pp_mlp.cu -- the learned surrogate: a small MLP trained and evaluated with
-// hand-written BF16 tcgen05 kernels (FP32 accumulation in tensor memory).
+// hand-written tcgen05 kernels (FP32 accumulation in tensor memory): BF16
+// operands for training, F16 for the fused inference kernel.
 //
 // No counterpart in the reference: PhotonPropagation.jl evaluates an external
 // surrogate (PhotonSurrogateModel, examples/validation.jl:455,673-676) whose
@@ -12,7 +13,8 @@
 // head (1 log-expected-count + 64 time logits, padded to 80).  Loss per sample
 // (Poisson + multinomial negative log-likelihood):
 //   L = exp(o0) - k*o0 - sum_b h_b * log softmax(o_1..64)_b.
-// Parameters are FP32 masters with BF16 copies for the tensor cores; Adam.
+// Parameters are FP32 masters with a BF16 copy for training and an F16 pack
+// for inference; Adam.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -178,7 +180,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constan
       for (int s = 0; s < kKC / 16 && k0 + s * 16 < kend; ++s) {
         const uint64_t ad = pptc::smem_desc(sa + s * 256, 128, 1024);
         const uint64_t bd = pptc::smem_desc(sb + s * 256, 128, 1024);
-        pptc::mma_bf16(tmem, ad, bd, idesc, st > 0 || s > 0);
+        pptc::mma_f16(tmem, ad, bd, idesc, st > 0 || s > 0);
       }
     }
   }
@@ -425,23 +427,28 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* _
 // ---------------------------------------------------------------------------
 // Fused inference.
 //
-// Weights are packed once per parameter update into K-chunks of kChunkK
-// columns (the last chunk of a layer may be 16 wide), each chunk a contiguous
-// block in the tensor core's core-matrix layout: element (r, c) of layer l
-// (rows x cols) at
+// The inference network runs in half precision (F16 operands, FP32
+// accumulators): F16 keeps three more mantissa bits than BF16 over the range
+// a trained network's activations take (|activation| < 32,768), and its packed
+// pair arithmetic halves the SFU work of the SiLU epilogue.  Weights are
+// packed once per parameter update from the FP32 parameters, the hidden
+// layers' scaled by 1/2 so that the accumulator is z/2 - b/2 (the argument of
+// silu(z) = h + h tanh(h), h = z/2), into K-chunks of kChunkK columns (the
+// last chunk of a layer may be 16 wide), each chunk a contiguous block in the
+// tensor core's core-matrix layout: element (r, c) of layer l (rows x cols) at
 //   wpack_off[l] + (c / kChunkK) * rows * kChunkK * 2
 //   + core_offset(r, (c % kChunkK) / 8, chunk width) + (c % 8) * 2,
 // so that one TMA bulk copy brings one chunk into a ring slot.
 constexpr int kChunkK = 64;
 constexpr int kRingSlots = 3;
-constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 64 BF16
+constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 64 16-bit values
 constexpr uint32_t kRedBytes = 2u * 4u * 128u * 4u;   // head: row max and sum per column group
 
 __host__ __device__ inline int chunk_width(int K, int j) {
   return K - j * kChunkK < kChunkK ? K - j * kChunkK : kChunkK;
 }
 
-__global__ void repack_kernel(const bf16* __restrict__ w, int rows, int cols,
+__global__ void repack_kernel(const float* __restrict__ w, int rows, int cols, float scale,
                               unsigned char* __restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (long long)rows * cols) return;
@@ -449,7 +456,13 @@ __global__ void repack_kernel(const bf16* __restrict__ w, int rows, int cols,
   const int j = c / kChunkK, cc = c % kChunkK;
   const size_t off = (size_t)j * rows * kChunkK * 2 +
                      pptc::core_offset(r, cc >> 3, chunk_width(cols, j)) + (cc & 7) * 2;
-  *reinterpret_cast<bf16*>(out + off) = w[i];
+  *reinterpret_cast<__half*>(out + off) = __float2half_rn(w[i] * scale);
+}
+
+// b / 2 of a hidden layer in half precision (the epilogue's bias table).
+__global__ void half_bias_kernel(const float* __restrict__ b, int n, __half* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = __float2half_rn(0.5f * b[i]);
 }
 
 constexpr int kMaxLayers = 17;
@@ -463,12 +476,13 @@ struct InferParams {
   int n_in, in_pad, hidden, n_layers, out_pad, n_bins;
   int n_tiles, n_rounds;
   uint32_t slot_cols;               // TMEM columns per accumulator (power of two >= 32)
-  uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) BF16)
+  uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) F16)
   uint32_t ring_off;                // shared-memory byte offset of the weight ring
   int stage_pdf;                    // PDF rows staged through shared memory
   const unsigned char* wpack;
   long long wpack_off[kMaxLayers];  // bytes, multiples of 512
-  const float* P;                   // FP32 parameters (biases)
+  const __half* bias_half;          // hidden layer l: b / 2 at l * hidden
+  const float* P;                   // FP32 parameters (the head's biases)
   long long off_b[kMaxLayers];
   float* expect;                    // [n]
   float* pdf;                       // [n x n_bins], may be null
@@ -527,13 +541,9 @@ __device__ __forceinline__ void load_unit(const InferParams& p, int tile, int u,
 }
 __device__ __forceinline__ void store_unit(const InferParams& p, unsigned char* act, int u,
                                            const float* xin) {
-  union {
-    uint4 u4;
-    __nv_bfloat162 h2[4];
-  } v;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) v.h2[j] = __floats2bfloat162_rn(xin[2 * j], xin[2 * j + 1]);
-  *reinterpret_cast<uint4*>(act + pptc::core_offset(u & 127, u >> 7, p.in_pad)) = v.u4;
+  const uint4 v = make_uint4(pptc::f16x2_from(xin[0], xin[1]), pptc::f16x2_from(xin[2], xin[3]),
+                             pptc::f16x2_from(xin[4], xin[5]), pptc::f16x2_from(xin[6], xin[7]));
+  *reinterpret_cast<uint4*>(act + pptc::core_offset(u & 127, u >> 7, p.in_pad)) = v;
 }
 __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* act, int tile,
                                            int t) {
@@ -545,26 +555,28 @@ __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* 
 }
 
 // Bias + SiLU of one 32-column slice (columns cb .. cb + 31 of this thread's
-// row) into the BF16 activations; bl2 holds bias / 2 of column cb + lane.
+// row) into the F16 activations, in packed pairs: h = acc + b/2 (the
+// accumulator holds z/2 - b/2), silu = h + h tanh(h).  bh is the layer's b/2
+// table (8 columns per 16-byte load, the same address in every lane).
 // kFull: all 32 columns exist (no bound checks, fully interleavable).
 template <bool kFull>
-__device__ __forceinline__ void silu_slice(const uint32_t* v, float bl2, int cb, int hidden,
-                                           unsigned char* act, int r) {
+__device__ __forceinline__ void silu_slice(const uint32_t* v, const uint4* __restrict__ bh, int cb,
+                                           int hidden, unsigned char* act, int r) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     if (!kFull && cb + q * 8 >= hidden) break;
-    union {
-      uint4 u4;
-      __nv_bfloat162 h2[4];
-    } o;
+    const uint4 b4 = __ldg(bh + (cb >> 3) + q);
+    const uint32_t bb[4] = {b4.x, b4.y, b4.z, b4.w};
+    uint32_t o[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int i = q * 8 + 2 * j;
-      const float h0 = fmaf(__uint_as_float(v[i]), 0.5f, __shfl_sync(0xffffffffu, bl2, i));
-      const float h1 = fmaf(__uint_as_float(v[i + 1]), 0.5f, __shfl_sync(0xffffffffu, bl2, i + 1));
-      o.h2[j] = __floats2bfloat162_rn(pptc::silu_half(h0), pptc::silu_half(h1));
+      const uint32_t h = pptc::f16x2_add(
+          pptc::f16x2_from(__uint_as_float(v[i]), __uint_as_float(v[i + 1])), bb[j]);
+      o[j] = pptc::f16x2_fma(h, pptc::f16x2_tanh(h), h);
     }
-    *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, hidden)) = o.u4;
+    *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, hidden)) =
+        make_uint4(o[0], o[1], o[2], o[3]);
   }
 }
 
@@ -694,7 +706,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         // address field (shared addresses < 256 KB: the field never carries)
         const uint64_t a_desc = pptc::smem_desc(pptc::smem_u32(smem + (size_t)T * p.act_bytes), 128,
                                                 (uint32_t)(K / 8) * 128u);
-        const uint32_t idesc = pptc::idesc_bf16(128, N);
+        const uint32_t idesc = pptc::idesc_f16(128, N);
         for (int j = 0; j * kChunkK < K; ++j, ++k) {
           const uint32_t slot = k % kRingSlots, use = k / kRingSlots;
           if (abort_flag || !pptc::mbar_wait(&w_full[slot], use & 1, kWaitNs)) {
@@ -707,7 +719,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
               pptc::smem_desc(pptc::smem_u32(ring + slot * kSlotBytes), 128, (uint32_t)(w / 8) * 128u);
           const uint64_t a_j = a_desc + (uint64_t)(j * (kChunkK / 16) * 16);  // + j * 64 cols * 2 B / 16
           for (int s = 0; s < w / 16; ++s)
-            pptc::mma_bf16(d, a_j + (uint64_t)(s * 16), b_desc + (uint64_t)(s * 16), idesc,
+            pptc::mma_f16(d, a_j + (uint64_t)(s * 16), b_desc + (uint64_t)(s * 16), idesc,
                            j > 0 || s > 0);
           // the slot is free (in every CTA's view) once these MMAs complete
           pptc::mma_commit_multicast(&w_empty[slot], (uint16_t)((1u << kCluster) - 1u));
@@ -742,14 +754,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     while (more) {
       const int T = it.slot, l = it.layer;
       unsigned char* act = smem + (size_t)T * p.act_bytes;
-      // this lane's bias values of the job's two column slices, loaded before
-      // the wait (the inner loops broadcast them by shuffle)
+      // head: this lane's bias values of the job's two column slices, loaded
+      // before the wait (the inner loops broadcast them by shuffle)
+      const bool head = l == p.n_layers;
       const float* __restrict__ bias = p.P + p.off_b[l];
-      const int width = l < p.n_layers ? p.hidden : p.out_pad;
-      const int s0 = cgrp * 32;
-      const int s1 = l < p.n_layers ? cgrp * 32 + 128 : (cgrp + 4) * 32;
-      const float bl0 = s0 + lane < width ? __ldg(bias + s0 + lane) : 0.0f;
-      const float bl1 = s1 + lane < width ? __ldg(bias + s1 + lane) : 0.0f;
+      const int s0 = cgrp * 32, s1 = (cgrp + 4) * 32;
+      const float bl0 = head && s0 + lane < p.out_pad ? __ldg(bias + s0 + lane) : 0.0f;
+      const float bl1 = head && s1 + lane < p.out_pad ? __ldg(bias + s1 + lane) : 0.0f;
       if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, kWaitNs))) {
         ok = false;
         break;
@@ -765,13 +776,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           pptc::tmem_ld32_nowait(trow + (uint32_t)c0, v[0]);
           if (two) pptc::tmem_ld32_nowait(trow + (uint32_t)(c0 + 128), v[1]);
           pptc::tmem_wait();
+          const uint4* bh = reinterpret_cast<const uint4*>(p.bias_half + (size_t)l * p.hidden);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             if (h == 1 && !two) break;
             const int cb = c0 + h * 128;
-            const float bl2 = 0.5f * (h ? bl1 : bl0);
-            if (cb + 32 <= p.hidden) silu_slice<true>(v[h], bl2, cb, p.hidden, act, r);
-            else silu_slice<false>(v[h], bl2, cb, p.hidden, act, r);
+            if (cb + 32 <= p.hidden) silu_slice<true>(v[h], bh, cb, p.hidden, act, r);
+            else silu_slice<false>(v[h], bh, cb, p.hidden, act, r);
           }
         }
       } else {
@@ -940,7 +951,8 @@ struct pp_mlp {
   bf16* dZ[2] = {nullptr, nullptr};
   float* loss = nullptr;
   unsigned* err = nullptr;
-  unsigned char* wpack = nullptr;       // BF16 weights in core-matrix layout
+  unsigned char* wpack = nullptr;       // F16 weights in core-matrix layout
+  __half* bias_half = nullptr;          // b / 2 of the hidden layers, F16
   std::vector<long long> wpack_off;     // bytes per layer
   bool pack_dirty = true;
   int num_sms = 0;
@@ -975,6 +987,7 @@ void mlp_free(pp_mlp* m) {
   cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16); cudaFree(m->dO32);
   cudaFree(m->dZ[0]); cudaFree(m->dZ[1]); cudaFree(m->loss); cudaFree(m->err);
   cudaFree(m->wpack);
+  cudaFree(m->bias_half);
   cudaFree(m->bx); cudaFree(m->bc); cudaFree(m->bh); cudaFree(m->d_step); cudaFree(m->d_sched);
   if (m->step_graph) cudaGraphExecDestroy(m->step_graph);
   if (m->cap_stream) cudaStreamDestroy(m->cap_stream);
@@ -1078,8 +1091,13 @@ int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cu
 int mlp_repack(pp_mlp* m, cudaStream_t s) {
   for (int l = 0; l <= m->n_layers; ++l) {
     const long long n = (long long)m->rows[l] * m->cols[l];
-    repack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(m->P16 + m->off_w[l], m->rows[l],
-                                                            m->cols[l], m->wpack + m->wpack_off[l]);
+    const bool hidden = l < m->n_layers;
+    repack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        m->P + m->off_w[l], m->rows[l], m->cols[l], hidden ? 0.5f : 1.0f,
+        m->wpack + m->wpack_off[l]);
+    if (hidden)
+      half_bias_kernel<<<(unsigned)((m->hidden + 255) / 256), 256, 0, s>>>(
+          m->P + m->off_b[l], m->hidden, m->bias_half + (size_t)l * m->hidden);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "repack weights");
@@ -1088,7 +1106,7 @@ int mlp_repack(pp_mlp* m, cudaStream_t s) {
 }
 
 // Shared memory of infer_kernel: the activations of two tiles (128 rows x
-// max(in_pad, hidden) BF16 each, at least the head's reduction arrays), then
+// max(in_pad, hidden) F16 each, at least the head's reduction arrays), then
 // the weight ring.  The head stages a tile's PDF rows (128 x (n_bins + 1)
 // floats) in that tile's activation buffer when they fit before the
 // reduction arrays at its end.
@@ -1198,6 +1216,7 @@ PP_API int pp_mlp_create(pp_mlp** out, int32_t device, int32_t n_in, int32_t hid
     wbytes += (long long)m->rows[l] * m->cols[l] * 2;  // rows, cols multiples of 16: 512-byte steps
   }
   A((void**)&m->wpack, (size_t)wbytes);
+  A((void**)&m->bias_half, sizeof(__half) * (size_t)n_layers * hidden);
   if (e == cudaSuccess) e = cudaMemcpy(m->P, h.data(), pb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->Mo, 0, pb);
   if (e == cudaSuccess) e = cudaMemset(m->Vo, 0, pb);
@@ -1452,7 +1471,7 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
   while (p.slot_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.slot_cols *= 2;
   p.act_bytes = sm.act; p.ring_off = sm.ring_off;
   p.stage_pdf = sm.stage_pdf ? 1 : 0;
-  p.wpack = m->wpack; p.P = m->P;
+  p.wpack = m->wpack; p.bias_half = m->bias_half; p.P = m->P;
   for (int l = 0; l <= m->n_layers; ++l) {
     p.wpack_off[l] = m->wpack_off[l];
     p.off_b[l] = m->off_b[l];

@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -48,6 +49,35 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
          | ((uint32_t)(m >> 4) << 24);  // M >> 4
 }
 
+// The same with F16 A and B.
+__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
+  return (1u << 4)                      // D format: F32
+         | ((uint32_t)(n >> 3) << 17)   // N >> 3 (A and B format fields 0: F16)
+         | ((uint32_t)(m >> 4) << 24);  // M >> 4
+}
+
+// Packed half-precision pairs (low half = the first element).
+__device__ __forceinline__ uint32_t f16x2_from(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+__device__ __forceinline__ uint32_t f16x2_add(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+__device__ __forceinline__ uint32_t f16x2_fma(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+__device__ __forceinline__ uint32_t f16x2_tanh(uint32_t a) {
+  uint32_t d;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(d) : "r"(a));
+  return d;
+}
+
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                    smem_u32(dst_smem)),
@@ -73,7 +103,7 @@ __device__ __forceinline__ void fence_async_smem() {
 }
 
 // D (+)= A * B^T for one M=128 x N tile and K = 16.
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
                                          uint32_t idesc, bool accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"

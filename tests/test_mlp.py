@@ -155,13 +155,18 @@ def test_fused_inference_matches_oracle(pp, gpu_ctx, n, hidden, layers, n_bins):
     pdf = torch.full((n, n_bins), -1.0, device="cuda")
     mlp.infer(xd.data_ptr(), n, expect.data_ptr(), pdf.data_ptr())
     W, b = mlp.unpack(mlp.params())
-    lam, p_ref = mlp_oracle.MLPOracle(W, b, 8, n_bins).predict(x)
+    lam, p_ref = mlp_oracle.MLPOracle(W, b, 8, n_bins, half=True).predict(x)
     got_l, got_p = expect.cpu().numpy(), pdf.cpu().numpy()
-    # BF16 activations (one rounding flip moves an output by ~1e-3) and the
-    # tanh.approx sigmoid (~2^-11): the log-count output agrees within 1e-2
+    # F16 activations and weights, the SiLU in packed half arithmetic with
+    # tanh.approx.f16x2 (~2^-11 relative): against the oracle's F16 rounding
+    # points the log-count output agrees within 1e-2, the PDF within 1%
     np.testing.assert_allclose(np.log(got_l), np.log(lam), atol=1e-2)
     np.testing.assert_allclose(got_p.sum(axis=1), 1.0, rtol=1e-5)
     np.testing.assert_allclose(got_p, p_ref, rtol=1e-2, atol=1e-5)
+    # and the exact (FP64) network within the same bounds
+    lam64, p64 = mlp_oracle.MLPOracle(W, b, 8, n_bins, round_bf16=False).predict(x)
+    np.testing.assert_allclose(np.log(got_l), np.log(lam64), atol=1e-2)
+    np.testing.assert_allclose(got_p, p64, rtol=1e-2, atol=1e-5)
     # the expected counts alone (no PDF output)
     e2 = torch.zeros(n, device="cuda")
     mlp.infer(xd.data_ptr(), n, e2.data_ptr())
@@ -183,7 +188,7 @@ def test_fused_inference_follows_training(pp, gpu_ctx):
     mlp.infer(dev[0].data_ptr(), B, e1.data_ptr())
     assert not torch.equal(e0, e1)
     W, b = mlp.unpack(mlp.params())
-    lam, _ = mlp_oracle.MLPOracle(W, b, 8, 64).predict(x)
+    lam, _ = mlp_oracle.MLPOracle(W, b, 8, 64, half=True).predict(x)
     np.testing.assert_allclose(np.log(e1.cpu().numpy()), np.log(lam), atol=1e-2)
     mlp.close()
 
