@@ -293,8 +293,7 @@ LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_reco
   a.mono_wavelength = ctx->mono;
   a.track = ctx->d_track;
   a.n_track = ctx->n_track;
-  a.key0 = (uint32_t)((unsigned long long)seed & 0xffffffffu);
-  a.key1 = (uint32_t)((unsigned long long)seed >> 32);
+  a.set_seed((uint64_t)seed);
   a.n_steps = n_steps;
   a.hits = hits;
   a.capacity = capacity > 0 ? (unsigned long long)capacity : 0ull;

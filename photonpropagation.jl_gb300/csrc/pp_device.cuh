@@ -43,6 +43,18 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
+// The same with the ten rounds' keys given (key + r * (W0, W1), r = 0..9).
+__device__ __forceinline__ uint4 philox(uint4 c, const uint32_t* __restrict__ rk) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned long long p0 = (unsigned long long)kPhiloxM0 * c.x;
+    const unsigned long long p1 = (unsigned long long)kPhiloxM1 * c.z;
+    c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ rk[2 * r], (uint32_t)p1,
+                   (uint32_t)(p0 >> 32) ^ c.w ^ rk[2 * r + 1], (uint32_t)p0);
+  }
+  return c;
+}
+
 // 24-bit uniform in (0, 1] (exact: integer <= 2^24 times 2^-24).
 __device__ __forceinline__ float u01(uint32_t x) {
   return __uint2float_rn((x >> 8) + 1u) * 5.9604644775390625e-8f;
@@ -357,25 +369,23 @@ __device__ __forceinline__ int first_hit(const pp::GridDev& g, const uint32_t* _
         }
       }
     }
-    if (tnx <= tny && tnx <= tnz) {
-      if (tnx > tmax) break;
-      cx += sx;
-      if ((unsigned)cx >= (unsigned)nx) break;
-      tnx += tdx;
-      cidx += strx;
-    } else if (tny <= tnz) {
-      if (tny > tmax) break;
-      cy += sy;
-      if ((unsigned)cy >= (unsigned)ny) break;
-      tny += tdy;
-      cidx += stry;
-    } else {
-      if (tnz > tmax) break;
-      cz += sz;
-      if ((unsigned)cz >= (unsigned)nz) break;
-      tnz += tdz;
-      cidx += strz;
-    }
+    // the axis whose boundary comes first (x, then y, on ties), stepped by
+    // selects: lanes of a warp step different axes without diverging
+    const bool ax = tnx <= tny && tnx <= tnz;
+    const bool ay = !ax && tny <= tnz;
+    const bool az = !ax && !ay;
+    const float tn = ax ? tnx : (ay ? tny : tnz);
+    if (tn > tmax) break;
+    cx += ax ? sx : 0;
+    cy += ay ? sy : 0;
+    cz += az ? sz : 0;
+    if ((unsigned)cx >= (unsigned)nx || (unsigned)cy >= (unsigned)ny ||
+        (unsigned)cz >= (unsigned)nz)
+      break;
+    tnx += ax ? tdx : 0.0f;
+    tny += ay ? tdy : 0.0f;
+    tnz += az ? tdz : 0.0f;
+    cidx += ax ? strx : (ay ? stry : strz);
   }
   if (best == 0x7fffffff) return -1;
   *d_out = best_d;

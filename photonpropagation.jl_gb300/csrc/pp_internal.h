@@ -144,7 +144,20 @@ struct LaunchArgs {
   int n_track;
 
   uint32_t key0, key1;                     // Philox key = seed
+  uint32_t round_keys[20];                 // Philox round keys (set_seed)
   int n_steps;
+
+  // key = seed; round r of Philox4x32-10 uses (key0 + r W0, key1 + r W1),
+  // precomputed once per launch so that the per-step generator takes them as
+  // kernel-parameter operands instead of recomputing them
+  void set_seed(uint64_t seed) {
+    key0 = (uint32_t)(seed & 0xffffffffu);
+    key1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+      round_keys[2 * r] = key0 + (uint32_t)r * 0x9E3779B9u;
+      round_keys[2 * r + 1] = key1 + (uint32_t)r * 0xBB67AE85u;
+    }
+  }
 
   pp_hit_record* hits;
   unsigned long long capacity;

@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
       // Lanes past the end replay the first photon of the round (never recorded).
       const long long p = first + (active ? base + lane : base);
       const uint32_t plo = (uint32_t)p, phi = (uint32_t)((unsigned long long)p >> 32);
-      const uint4 r0 = philox(make_uint4(plo, phi, 0u, (uint32_t)s), a.key0, a.key1);
+      const uint4 r0 = philox(make_uint4(plo, phi, 0u, (uint32_t)s), a.round_keys);
       const float u0 = u01(r0.x), u1 = u01(r0.y), u2 = u01(r0.z), u3 = u01(r0.w);
       const float wl = a.spectrum ? spectrum_sample(a.spectrum, a.n_spectrum, u0)
                                   : a.mono_wavelength;
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
                                            (uint32_t)s, a.key0, a.key1) *
                     __ldg(&sp->long_lrad);
           } else if (kind == PP_SRC_CHERENKOV_TRACK) {
-            const uint4 re = philox(make_uint4(plo, phi, kExtraCall, (uint32_t)s), a.key0, a.key1);
+            const uint4 re = philox(make_uint4(plo, phi, kExtraCall, (uint32_t)s), a.round_keys);
             along = uniform_ab(0.0f, __ldg(&sp->length), u01(re.x));
           }
           if (kind != PP_SRC_POINTLIKE_CHERENKOV) {
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
       int count = 0;  // warp-uniform length of the deferred-segment queue
       bool found = false;  // shaped targets: the photon has hit
       for (int k = 1; k <= a.n_steps; ++k) {
-        const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.key0, a.key1);
+        const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.round_keys);
         const float step = -f_log<kPrecise>(u01(r.x)) * sca_len;
         if constexpr (kShapes) {
           if (active && !found) {

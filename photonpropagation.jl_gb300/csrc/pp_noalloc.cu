@@ -323,8 +323,7 @@ extern "C" PP_API int pp_propagate_static(
   a.mono_wavelength = mono_wavelength;
   a.track = needs_track ? d_track : nullptr;
   a.n_track = n_track;
-  a.key0 = (uint32_t)((unsigned long long)seed & 0xffffffffu);
-  a.key1 = (uint32_t)((unsigned long long)seed >> 32);
+  a.set_seed((uint64_t)seed);
   a.n_steps = n_steps;
   a.hits = d_hits;
   a.capacity = (unsigned long long)capacity;
