@@ -554,25 +554,33 @@ __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* 
   }
 }
 
+// b/2 of columns cb + 2 (lane % 16) and + 1 as a packed pair (0 past the
+// layer's width): the bias operand of silu_slice, loaded before the
+// accumulator wait so that its latency is hidden.
+__device__ __forceinline__ uint32_t bias_pair(const __half* __restrict__ bh, int cb, int hidden,
+                                              int lane) {
+  const int c = cb + 2 * (lane & 15);
+  return c < hidden ? __ldg(reinterpret_cast<const uint32_t*>(bh + c)) : 0u;
+}
+
 // Bias + SiLU of one 32-column slice (columns cb .. cb + 31 of this thread's
 // row) into the F16 activations, in packed pairs: h = acc + b/2 (the
-// accumulator holds z/2 - b/2), silu = h + h tanh(h).  bh is the layer's b/2
-// table (8 columns per 16-byte load, the same address in every lane).
+// accumulator holds z/2 - b/2), silu = h + h tanh(h).  bp is this lane's
+// bias_pair of the slice; pair k is broadcast from lane k.
 // kFull: all 32 columns exist (no bound checks, fully interleavable).
 template <bool kFull>
-__device__ __forceinline__ void silu_slice(const uint32_t* v, const uint4* __restrict__ bh, int cb,
-                                           int hidden, unsigned char* act, int r) {
+__device__ __forceinline__ void silu_slice(const uint32_t* v, uint32_t bp, int cb, int hidden,
+                                           unsigned char* act, int r) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     if (!kFull && cb + q * 8 >= hidden) break;
-    const uint4 b4 = __ldg(bh + (cb >> 3) + q);
-    const uint32_t bb[4] = {b4.x, b4.y, b4.z, b4.w};
     uint32_t o[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int i = q * 8 + 2 * j;
       const uint32_t h = pptc::f16x2_add(
-          pptc::f16x2_from(__uint_as_float(v[i]), __uint_as_float(v[i + 1])), bb[j]);
+          pptc::f16x2_from(__uint_as_float(v[i]), __uint_as_float(v[i + 1])),
+          __shfl_sync(0xffffffffu, bp, q * 4 + j));
       o[j] = pptc::f16x2_fma(h, pptc::f16x2_tanh(h), h);
     }
     *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, hidden)) =
@@ -688,41 +696,58 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
+      // The issue loop is kept short: the tensor core runs a 128x256x16 MMA
+      // in ~128 cycles, and this one thread's bookkeeping between MMAs (waits,
+      // descriptors, loop control) must fit in that time or the pipe idles.
       JobIter it;
       bool more = it.next(p);
-      uint32_t k = 0;                   // chunks consumed
+      uint32_t slot = 0, phase = 0;     // ring slot of the next chunk, its fill parity
       uint32_t jobs[2] = {0u, 0u};      // jobs issued per slot
+      // descriptor of ring slot 0 holding a full-width chunk; descriptors
+      // advance by adding the byte offset / 16 to the start address field
+      // (shared addresses < 256 KB: the field never carries)
+      const uint64_t b_full = pptc::smem_desc(pptc::smem_u32(ring), 128, (uint32_t)(kChunkK / 8) * 128u);
+      const uint32_t idesc_hidden = pptc::idesc_f16(128, p.hidden);
+      const uint32_t idesc_head = pptc::idesc_f16(128, p.out_pad);
       while (more && ok) {
         const int T = it.slot, l = it.layer;
         const int K = l == 0 ? p.in_pad : p.hidden;
-        const int N = l == p.n_layers ? p.out_pad : p.hidden;
         if (abort_flag || !pptc::mbar_wait(&act_ready[T], jobs[T] & 1, kWaitNs)) {
           ok = false;
           break;
         }
         pptc::fence_after_sync();
         const uint32_t d = tmem + (uint32_t)T * p.slot_cols;
-        // descriptors advance by adding the byte offset / 16 to the start
-        // address field (shared addresses < 256 KB: the field never carries)
         const uint64_t a_desc = pptc::smem_desc(pptc::smem_u32(smem + (size_t)T * p.act_bytes), 128,
                                                 (uint32_t)(K / 8) * 128u);
-        const uint32_t idesc = pptc::idesc_f16(128, N);
-        for (int j = 0; j * kChunkK < K; ++j, ++k) {
-          const uint32_t slot = k % kRingSlots, use = k / kRingSlots;
-          if (abort_flag || !pptc::mbar_wait(&w_full[slot], use & 1, kWaitNs)) {
+        const uint32_t idesc = l == p.n_layers ? idesc_head : idesc_hidden;
+        for (int j = 0; j * kChunkK < K; ++j) {
+          if (!pptc::mbar_wait(&w_full[slot], phase, kWaitNs) || abort_flag) {
             ok = false;
             break;
           }
           pptc::fence_after_sync();
-          const int w = chunk_width(K, j);
-          const uint64_t b_desc =
-              pptc::smem_desc(pptc::smem_u32(ring + slot * kSlotBytes), 128, (uint32_t)(w / 8) * 128u);
           const uint64_t a_j = a_desc + (uint64_t)(j * (kChunkK / 16) * 16);  // + j * 64 cols * 2 B / 16
-          for (int s = 0; s < w / 16; ++s)
-            pptc::mma_f16(d, a_j + (uint64_t)(s * 16), b_desc + (uint64_t)(s * 16), idesc,
-                           j > 0 || s > 0);
+          const int w = chunk_width(K, j);
+          if (w == kChunkK) {
+            const uint64_t b = b_full + (uint64_t)(slot * (kSlotBytes / 16));
+#pragma unroll
+            for (int s = 0; s < kChunkK / 16; ++s)
+              pptc::mma_f16(d, a_j + (uint64_t)(s * 16), b + (uint64_t)(s * 16), idesc,
+                            j > 0 || s > 0);
+          } else {
+            const uint64_t b = pptc::smem_desc(pptc::smem_u32(ring + slot * kSlotBytes), 128,
+                                               (uint32_t)(w / 8) * 128u);
+            for (int s = 0; s < w / 16; ++s)
+              pptc::mma_f16(d, a_j + (uint64_t)(s * 16), b + (uint64_t)(s * 16), idesc,
+                            j > 0 || s > 0);
+          }
           // the slot is free (in every CTA's view) once these MMAs complete
           pptc::mma_commit_multicast(&w_empty[slot], (uint16_t)((1u << kCluster) - 1u));
+          if (++slot == kRingSlots) {
+            slot = 0;
+            phase ^= 1u;
+          }
         }
         if (!ok) break;
         pptc::mma_commit(&acc_full[T]);
@@ -754,13 +779,17 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     while (more) {
       const int T = it.slot, l = it.layer;
       unsigned char* act = smem + (size_t)T * p.act_bytes;
-      // head: this lane's bias values of the job's two column slices, loaded
-      // before the wait (the inner loops broadcast them by shuffle)
+      // this lane's bias values of the job's two column slices, loaded
+      // before the wait (the inner loops broadcast them by shuffle): FP32
+      // for the head, packed b/2 pairs for a hidden layer
       const bool head = l == p.n_layers;
       const float* __restrict__ bias = p.P + p.off_b[l];
       const int s0 = cgrp * 32, s1 = (cgrp + 4) * 32;
       const float bl0 = head && s0 + lane < p.out_pad ? __ldg(bias + s0 + lane) : 0.0f;
       const float bl1 = head && s1 + lane < p.out_pad ? __ldg(bias + s1 + lane) : 0.0f;
+      const __half* bh = p.bias_half + (size_t)l * p.hidden;
+      const uint32_t bp0 = head ? 0u : bias_pair(bh, s0, p.hidden, lane);
+      const uint32_t bp1 = head ? 0u : bias_pair(bh, s0 + 128, p.hidden, lane);
       if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, kWaitNs))) {
         ok = false;
         break;
@@ -776,13 +805,17 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           pptc::tmem_ld32_nowait(trow + (uint32_t)c0, v[0]);
           if (two) pptc::tmem_ld32_nowait(trow + (uint32_t)(c0 + 128), v[1]);
           pptc::tmem_wait();
-          const uint4* bh = reinterpret_cast<const uint4*>(p.bias_half + (size_t)l * p.hidden);
+          // (hidden <= 256: one pass with the preloaded pairs; wider layers
+          // load theirs here)
+          const uint32_t b0 = c0 == s0 ? bp0 : bias_pair(bh, c0, p.hidden, lane);
+          const uint32_t b1 = c0 == s0 ? bp1 : bias_pair(bh, c0 + 128, p.hidden, lane);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             if (h == 1 && !two) break;
             const int cb = c0 + h * 128;
-            if (cb + 32 <= p.hidden) silu_slice<true>(v[h], bh, cb, p.hidden, act, r);
-            else silu_slice<false>(v[h], bh, cb, p.hidden, act, r);
+            const uint32_t bp = h ? b1 : b0;
+            if (cb + 32 <= p.hidden) silu_slice<true>(v[h], bp, cb, p.hidden, act, r);
+            else silu_slice<false>(v[h], bp, cb, p.hidden, act, r);
           }
         }
       } else {

@@ -146,21 +146,29 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
-// Wait for phase `parity` of the mbarrier for at most limit_ns.
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Wait for phase `parity` of the mbarrier for at most limit_ns.  A phase that
+// has already completed costs one try_wait: the clock is read only when the
+// first try fails (a single-thread MMA issuer has about 128 cycles per
+// 128x256x16 MMA for all of its bookkeeping).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
                                           unsigned long long limit_ns) {
   const uint32_t a = smem_u32(bar);
+  if (mbar_try(a, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (true) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
+    if (mbar_try(a, parity)) return true;
     if (gtimer() - t0 > limit_ns) return false;
   }
 }
