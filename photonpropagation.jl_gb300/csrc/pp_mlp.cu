@@ -443,6 +443,8 @@ constexpr int kChunkK = 64;
 constexpr int kRingSlots = 3;
 constexpr uint32_t kSlotBytes = 256u * kChunkK * 2u;  // up to 256 rows x 64 16-bit values
 constexpr uint32_t kRedBytes = 2u * 4u * 128u * 4u;   // head: row max and sum per column group
+// one-pass head: max and sum per 16-column half and row, then the halves' scales
+constexpr uint32_t kHeadRedBytes = 3u * 8u * 128u * 4u;
 
 __host__ __device__ inline int chunk_width(int K, int j) {
   return K - j * kChunkK < kChunkK ? K - j * kChunkK : kChunkK;
@@ -466,6 +468,7 @@ __global__ void half_bias_kernel(const float* __restrict__ b, int n, __half* __r
 }
 
 constexpr int kMaxLayers = 17;
+constexpr size_t kMaxInferSmem = 232448 - 256;  // 227 KB opt-in less the static barriers
 constexpr int kEpiWarps = 16;                        // epilogue warps (4 per TMEM lane quarter)
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kInferThreads = 64 + kEpiThreads;      // producer warp, MMA warp, epilogue
@@ -478,6 +481,7 @@ struct InferParams {
   uint32_t slot_cols;               // TMEM columns per accumulator (power of two >= 32)
   uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) F16)
   uint32_t ring_off;                // shared-memory byte offset of the weight ring
+  uint32_t head_bias_off;           // offset of the head's FP32 biases (one-pass head), or 0
   int stage_pdf;                    // PDF rows staged through shared memory
   const unsigned char* wpack;
   long long wpack_off[kMaxLayers];  // bytes, multiples of 512
@@ -767,6 +771,11 @@ __global__ void __launch_bounds__(kInferThreads, 1)
     const int quad = warp & 3;  // TMEM lane quarter this warp may access
     const int cgrp = ew >> 2;   // column group 0..3
     const int r = quad * 32 + lane;
+    // the head's biases for the one-pass head (visible to every epilogue
+    // thread after the first epi_all barrier, long before the first head)
+    float* head_bias = reinterpret_cast<float*>(smem + p.head_bias_off);
+    if (p.head_bias_off)
+      for (int c = t; c < p.out_pad; c += kEpiThreads) head_bias[c] = p.P[p.off_b[p.n_layers] + c];
     // first tiles of both slots
     for (int T = 0; T < 2; ++T) {
       pack_input(p, smem + (size_t)T * p.act_bytes, (int)blockIdx.x * 2 + T, t);
@@ -833,10 +842,94 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         // the slot's next input, loaded now so that its latency overlaps the head
         const int next = tile + 2 * (int)gridDim.x;
         const int units = 16 * p.in_pad;  // 128 rows x in_pad / 8 chunks of 8
-        const bool prefetch = units <= kEpiThreads;
+        // one-pass head (PDF output requested and the layout allows it)
+        const bool one_pass = p.head_bias_off != 0 && p.pdf != nullptr;
+        const bool prefetch = units <= kEpiThreads && !one_pass;
         float xin[8];
         const bool more_rounds = it.round + 1 < p.n_rounds;
         if (prefetch && t < units && more_rounds) load_unit(p, next, t, xin);
+        if (one_pass) {
+          // one pass: this warp's 32-column slice (if any) is read once; each
+          // 16-column half's exponentials go to the staging rows relative to
+          // the half's own maximum, the halves' (max, sum) partials meet in
+          // shared memory, and the copy-out applies each half's scale
+          constexpr float kLog2e = 1.44269504f;
+          float(*h_max)[128] = reinterpret_cast<float(*)[128]>(act + p.act_bytes - kHeadRedBytes);
+          float(*h_sum)[128] = h_max + 8;
+          float* h_scale = reinterpret_cast<float*>(h_sum + 8);  // [128][8]
+          float o0 = 0.0f;
+          float mh[2] = {-INFINITY, -INFINITY}, sh[2] = {0.0f, 0.0f};
+          const int cb = cgrp * 32;
+          if (cb < p.out_pad) {
+            uint32_t e[32];  // columns cb .. cb + 31 (within the slot's accumulator)
+            pptc::tmem_ld32_nowait(trow + (uint32_t)cb, e);
+            pptc::tmem_wait();
+            const float4* hb = reinterpret_cast<const float4*>(head_bias + cb);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              if (cb + 4 * q < p.out_pad) {  // the bias table holds out_pad values
+                const float4 b = hb[q];
+                e[4 * q] = __float_as_uint(__uint_as_float(e[4 * q]) + b.x);
+                e[4 * q + 1] = __float_as_uint(__uint_as_float(e[4 * q + 1]) + b.y);
+                e[4 * q + 2] = __float_as_uint(__uint_as_float(e[4 * q + 2]) + b.z);
+                e[4 * q + 3] = __float_as_uint(__uint_as_float(e[4 * q + 3]) + b.w);
+              }
+            }
+            if (cb == 0) o0 = __uint_as_float(e[0]);
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              float m = -INFINITY, se = 0.0f;
+#pragma unroll
+              for (int i = 16 * hh; i < 16 * hh + 16; ++i) {
+                const int c = cb + i;
+                if (c >= 1 && c <= p.n_bins) m = fmaxf(m, __uint_as_float(e[i]));
+              }
+#pragma unroll
+              for (int i = 16 * hh; i < 16 * hh + 16; ++i) {
+                const int c = cb + i;
+                if (c >= 1 && c <= p.n_bins) {
+                  const float x = pptc::ex2_approx((__uint_as_float(e[i]) - m) * kLog2e);
+                  se += x;
+                  stage[r * ld + c - 1] = x;
+                }
+              }
+              mh[hh] = m;
+              sh[hh] = se;
+            }
+          }
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            h_max[cgrp * 2 + hh][r] = mh[hh];
+            h_sum[cgrp * 2 + hh][r] = sh[hh];
+          }
+          if (cgrp == 0 && row < p.n) p.expect[row] = __expf(fminf(o0, 30.0f));
+          epi_sync();
+          {
+            float M = -INFINITY;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) M = fmaxf(M, h_max[w][r]);
+            float S = 0.0f;
+#pragma unroll
+            for (int w = 0; w < 8; ++w) {
+              const float mw = h_max[w][r];
+              S += mw == -INFINITY ? 0.0f : h_sum[w][r] * pptc::ex2_approx((mw - M) * kLog2e);
+            }
+            // this warp's two halves: scale = 2^((m_h - M) log2 e) / S
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const float mh = h_max[cgrp * 2 + hh][r];
+              h_scale[r * 8 + cgrp * 2 + hh] =
+                  mh == -INFINITY ? 0.0f : __fdividef(pptc::ex2_approx((mh - M) * kLog2e), S);
+            }
+          }
+          epi_sync();
+          const long long left = p.n - row0;
+          const int nrows = left < 128 ? (int)left : 128;
+          float* dst = p.pdf + row0 * p.n_bins;
+          for (int rr = ew; rr < nrows; rr += kEpiWarps)
+            for (int c = lane; c < p.n_bins; c += 32)
+              dst[rr * p.n_bins + c] = stage[rr * ld + c] * h_scale[rr * 8 + ((c + 1) >> 4)];
+        } else {
         // pass 1: the log count and this warp's part of the row maximum
         float o0 = 0.0f, mx = -INFINITY;
 #pragma unroll 1
@@ -909,6 +1002,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
             }
           }
         }
+        }  // multi-pass head
         epi_sync();  // the slot's buffer is read out before the next input lands
         if (more_rounds) {
           if (prefetch) {
@@ -1146,13 +1240,20 @@ int mlp_repack(pp_mlp* m, cudaStream_t s) {
 struct InferSmem {
   uint32_t act, ring_off, total;
   bool stage_pdf;
+  uint32_t head_bias_off;  // 0: the multi-pass head
 };
 InferSmem infer_smem(const pp_mlp* m) {
   const size_t act = std::max<size_t>((size_t)128 * std::max(m->hidden, m->in_pad) * 2, kRedBytes);
   const size_t ring_off = 2 * act;
+  const size_t end = ring_off + (size_t)kRingSlots * kSlotBytes;
+  const bool stage = (size_t)128 * (m->n_bins + 1) * 4 + kRedBytes <= act;
+  // one-pass head: at most one 32-column slice per epilogue warp, PDF rows
+  // staged, and room for the head's biases after the ring
+  const bool one_pass = (size_t)128 * (m->n_bins + 1) * 4 + kHeadRedBytes <= act &&
+                        m->out_pad <= 128 && end + (size_t)m->out_pad * 4 <= (size_t)kMaxInferSmem;
   return {(uint32_t)act, (uint32_t)ring_off,
-          (uint32_t)(ring_off + (size_t)kRingSlots * kSlotBytes),
-          (size_t)128 * (m->n_bins + 1) * 4 + kRedBytes <= act};
+          (uint32_t)(one_pass ? end + (size_t)m->out_pad * 4 : end), stage,
+          one_pass ? (uint32_t)end : 0u};
 }
 
 int check_err(pp_mlp* m, cudaStream_t s) {
@@ -1502,7 +1603,7 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
   p.n_tiles = (int)tiles;
   p.slot_cols = 32;
   while (p.slot_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.slot_cols *= 2;
-  p.act_bytes = sm.act; p.ring_off = sm.ring_off;
+  p.act_bytes = sm.act; p.ring_off = sm.ring_off; p.head_bias_off = sm.head_bias_off;
   p.stage_pdf = sm.stage_pdf ? 1 : 0;
   p.wpack = m->wpack; p.bias_half = m->bias_half; p.P = m->P;
   for (int l = 0; l <= m->n_layers; ++l) {

@@ -270,3 +270,42 @@ def test_train_steps_argument_checks(pp):
     assert lib.pp_mlp_train_steps(z, z, z, z, 10, 8, 1, 0, 1, 1e-3, 1e-5, 0, z) != 0
     v = ctypes.c_int64()
     assert lib.pp_mlp_step_count(z, ctypes.byref(v)) != 0
+
+
+@pytest.mark.gpu
+def test_train_steps_recapture_and_mixing(pp, gpu_ctx):
+    """A new schedule or batch size recaptures the step; single host steps
+    between captured runs keep one Adam step count; bad arguments fail
+    without a step taken."""
+    torch = pytest.importorskip("torch")
+    n = 2048
+    x, count, hist, dev = _make(pp, n, seed=11)
+    ptrs = [t.data_ptr() for t in dev]
+    m = pp.surrogate.MLP(max_batch=512, seed=12)
+    m.train_steps(*ptrs, n, 256, 3, 0, 10, 1e-3, 1e-5, 1)
+    m.train_step(ptrs[0], ptrs[1], ptrs[2], 128, 1e-3)
+    m.train_steps(*ptrs, n, 512, 2, 0, 10, 2e-3, 1e-5, 1)   # new batch size and rate
+    m.train_steps(*ptrs, n, 512, 0, 0, 10, 2e-3, 1e-5, 1)   # zero steps: nothing happens
+    torch.cuda.synchronize()
+    assert m.step_count() == 6
+    assert np.isfinite(m.last_loss())
+    assert np.all(np.isfinite(m.params()))
+    with pytest.raises(RuntimeError):
+        m.train_steps(*ptrs, n, 1024, 1, 0, 10, 1e-3, 1e-5, 1)  # above max_batch
+    with pytest.raises(RuntimeError):
+        m.train_steps(*ptrs, 0, 256, 1, 0, 10, 1e-3, 1e-5, 1)   # no rows
+    assert m.step_count() == 6
+    m.close()
+
+
+@pytest.mark.gpu
+def test_train_logs_every_point(pp, gpu_ctx):
+    torch = pytest.importorskip("torch")
+    n = 1024
+    x, count, hist, dev = _make(pp, n, seed=13)
+    m = pp.surrogate.MLP(max_batch=256, seed=14)
+    log = pp.surrogate.train(m, dev[0], dev[1], dev[2], steps=23, batch=256, log_every=10)
+    assert [s for s, _ in log] == [0, 10, 20, 22]
+    assert m.step_count() == 23
+    assert all(np.isfinite(v) for _, v in log)
+    m.close()
