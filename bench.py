@@ -609,6 +609,8 @@ def run_ours(args):
     for s in setups:
         if world > 1:
             s.sources = shard_sources(s, rank, world)
+    if tuning is not None:  # the same autotuner, run once through the public API
+        pp.autotune(setups[0], 15, sample_photons=min(photons, 8_000_000), device=local)
     pp.propagate_photons(setups[0], hb)  # warm (uploads this setup)
     torch.cuda.synchronize()
     t0 = time.perf_counter()

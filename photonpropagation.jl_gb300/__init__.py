@@ -10,7 +10,7 @@ from . import _lib
 from .context import Context, debug_philox, device_memory, measure_fp32_peak
 from .medium import (C_VAC_M_NS, CascadiaMediumProperties, HomogenousIceProperties,
                      MediumProperties, SimpleMediumProperties, make_homogenous_clearice_properties)
-from .processing import (HitBuffers, HitTable, PhotonPropOOMException, add_pmt_noise,
+from .processing import (HitBuffers, HitTable, PhotonPropOOMException, add_pmt_noise, autotune,
                          calc_number_of_steps, calc_total_weight, get_context, get_pmt_count,
                          make_hit_buffers, propagate_photons, resample_hits,
                          run_photon_prop_no_local_cache)

@@ -95,6 +95,22 @@ def _run(setup, hit_buffers: HitBuffers, n_steps: int):
     return ctx.fetch_hits(n_hits), n_ph_sim
 
 
+def autotune(setup, steps: int = 15, sample_photons: int = 8_000_000, device: int = 0) -> dict:
+    """Choose the launch shape (threads per block, photons per thread) and the
+    grid and safety-field cell sizes for `setup` by timing candidate
+    configurations on a photon sample (``pp_autotune``), and keep them on the
+    device's context: later ``propagate_photons`` calls on that device (any
+    setup) run with them.  The reference has no counterpart; its launch shape
+    is fixed.  Returns the chosen tuning and the sample's photons/s."""
+    ctx = get_context(device)
+    _ensure_uploaded(setup, ctx)
+    recs = setup.source_records()
+    ctx.set_sources(recs, len(setup.sources), setup.photon_scaling)
+    t, rate = ctx.autotune(setup.seed, steps, sample_photons=sample_photons)
+    return dict(block_threads=t.block_threads, photons_per_thread=t.photons_per_thread,
+                cell_size=t.cell_size, safety_cell=t.safety_cell, photons_per_s=rate)
+
+
 def run_photon_prop_no_local_cache(sources, targets, medium, spectrum, seed,
                                    hit_buffers: HitBuffers, n_steps: int = 15,
                                    photon_scaling: float = 1.0):

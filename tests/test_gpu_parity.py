@@ -322,3 +322,25 @@ def test_c1_full_size_properties(pp, orc, gpu_ctx):
     assert st["matched"] > 100, st
     rate_all, rate_or = nh / n, len(want) / m
     assert abs(rate_all - rate_or) < 5 * np.sqrt(rate_or / m), (rate_all, rate_or)
+
+
+def test_public_autotune_keeps_results(pp, gpu_ctx):
+    """pp.autotune tunes the context that propagate_photons uses; the hit
+    table is the same before and after (per-photon random streams)."""
+    setup = pp.workloads.c1_setup(photons=2_000_000, seed=2)
+    before = pp.propagate_photons(setup)
+    orig = gpu_ctx.get_tuning()
+    try:
+        t = pp.autotune(setup, 15, sample_photons=1_000_000)
+        assert 64 <= t["block_threads"] <= 512 and t["block_threads"] % 32 == 0
+        assert t["photons_per_thread"] >= 1 and t["cell_size"] > 0 and t["photons_per_s"] > 0
+        after = pp.propagate_photons(setup)
+    finally:
+        gpu_ctx.set_tuning(block_threads=orig.block_threads,
+                           photons_per_thread=orig.photons_per_thread,
+                           cell_size=orig.cell_size, safety_cell=orig.safety_cell,
+                           ctas_per_sm=orig.ctas_per_sm)
+    assert after.nrow == before.nrow > 0
+    o1, o2 = np.argsort(before["photon_index"]), np.argsort(after["photon_index"])
+    for k in ("position", "direction", "time", "module_id", "n_steps"):
+        np.testing.assert_array_equal(before[k][o1], after[k][o2], err_msg=k)
