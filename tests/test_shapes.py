@@ -99,3 +99,30 @@ def test_shaped_targets_fast_kernel_counts(pp, orc, gpu_ctx):
         g = int((got["module_index"] == k).sum())
         w = int((want["module_index"] == k).sum())
         assert abs(g - w) <= 5 * np.sqrt(max(w, 1)) + 5, (k, g, w)
+
+
+@pytest.mark.gpu
+def test_autotune_with_shaped_targets(pp, gpu_ctx):
+    """The autotuner on a context holding a shaped-target list (no grid to
+    size) tunes the launch shape only, and the hits do not change."""
+    setup = _mixed_setup(pp, 400_000, seed=9)
+    ctx = pp.Context(0)
+    try:
+        setup.upload(ctx)
+        recs = setup.source_records()
+        ctx.set_sources(recs, len(setup.sources), setup.photon_scaling)
+        n = sum(pp.source_photons(s.photons, setup.photon_scaling) for s in setup.sources)
+        rc, nh, _ = ctx.propagate(recs, len(setup.sources), setup.seed, 15,
+                                  setup.photon_scaling, n)
+        before = ctx.fetch_hits(nh)
+        t, rate = ctx.autotune(setup.seed, 15, sample_photons=200_000)
+        assert rate > 0 and 64 <= t.block_threads <= 512
+        rc2, nh2, _ = ctx.propagate(recs, len(setup.sources), setup.seed, 15,
+                                    setup.photon_scaling, n)
+        after = ctx.fetch_hits(nh2)
+    finally:
+        ctx.close()
+    assert rc == rc2 == 0 and nh == nh2 > 0
+    o1, o2 = np.argsort(before["photon_index"]), np.argsort(after["photon_index"])
+    for k in ("position", "module_index", "n_steps"):
+        np.testing.assert_array_equal(before[k][o1], after[k][o2], err_msg=k)
