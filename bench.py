@@ -11,7 +11,9 @@ Cascadia water, seeds 1..5 (one emitter position per seed; step k uses seed
          writing a 512 MiB buffer).
   e2e    photons/s through the public API call a user makes
          (propagate_photons(setup, hit_buffers)): source upload, kernel,
-         counters and the hit rows copied back to host memory, hit table built.
+         counters and the hit rows copied back to host memory, hit table built;
+         the context is tuned once beforehand with pp.autotune(setup), outside
+         the timed region (skipped with --no-autotune).
   roofline  FP32-issue bound: algorithmic FLOPs of the photon steps taken
          (device counter) / kernel time against a measured FFMA peak.
   cpu_baseline  the CPU oracle (a C restatement of the reference's step
@@ -658,7 +660,8 @@ def run_ours(args):
         },
         "e2e": {"value": e2e_value, "unit": "photons/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps,
-                "api": "propagate_photons(setup, hit_buffers) -> hit table in host memory"},
+                "api": "propagate_photons(setup, hit_buffers) -> hit table in host memory"
+                       + (" (context tuned once by pp.autotune(setup))" if tuning else "")},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      "traffic": traffic_full,
