@@ -309,3 +309,37 @@ def test_train_logs_every_point(pp, gpu_ctx):
     assert m.step_count() == 23
     assert all(np.isfinite(v) for _, v in log)
     m.close()
+
+
+def test_train_chunks_follow_log_points(pp):
+    """Host logic of surrogate.train: the captured steps run in chunks that end
+    at the log points, all with the same schedule (step0 = the Adam steps
+    taken before, total = steps)."""
+    torch = pytest.importorskip("torch")
+
+    class FakeMLP:
+        def __init__(self):
+            self.calls, self.steps = [], 7
+
+        def step_count(self):
+            return self.steps
+
+        def train_steps(self, x, c, h, n_rows, B, n_steps, step0, total, lr0, lr1, seed, stream):
+            self.calls.append((n_rows, B, n_steps, step0, total, lr0, lr1, seed))
+            self.steps += n_steps
+
+        def last_loss(self):
+            return float(self.steps)
+
+    x = torch.zeros(50, 8)
+    c = torch.zeros(50)
+    h = torch.zeros(50, 64)
+    m = FakeMLP()
+    log = pp.surrogate.train(m, x, c, h, steps=25, batch=16, lr=2e-3, seed=3, log_every=10)
+    assert [s for s, _ in log] == [0, 10, 20, 24]
+    assert [k[2] for k in m.calls] == [1, 10, 10, 4]
+    assert all(k[:2] == (50, 16) and k[3:] == (7, 25, 2e-3, 2e-5, 3) for k in m.calls)
+    assert m.steps == 7 + 25
+    m2 = FakeMLP()
+    assert pp.surrogate.train(m2, x, c, h, steps=5, batch=16) == []
+    assert [k[2] for k in m2.calls] == [5]
