@@ -418,6 +418,8 @@ PP_API int pp_mlp_set_adam(pp_mlp* mlp, const float* host_m, const float* host_v
 /* Fused inference (one tcgen05 kernel; activations stay in shared memory):
  * d_x (n x n_in, FP32, device) -> d_expect[n] = exp(min(log-count, 30)) and,
  * when d_pdf is not NULL, d_pdf (n x n_bins) = softmax of the time logits.
+ * Computed with F16 weights and activations (FP32 accumulation), so hidden
+ * activations must stay below 32,768 in magnitude.
  * Asynchronous on `stream`; n is not limited by max_batch.  Timeouts of the
  * kernel's waits set a device flag that pp_mlp_check reports. */
 PP_API int pp_mlp_infer(pp_mlp* mlp, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
