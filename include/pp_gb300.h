@@ -332,9 +332,8 @@ PP_API int pp_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_
 
 /* Propagation that allocates no device memory.  No counterpart in the
  * reference: it is for callers that cannot call cudaMalloc -- code running
- * while another framework's pooling allocator owns the device memory, code
- * recorded into a CUDA graph by its caller, services that fix their memory
- * use at start-up.  Inputs are host arrays (medium tables, spectrum knots or
+ * while another framework's pooling allocator owns the device memory, and
+ * services that fix their memory use at start-up.  Inputs are host arrays (medium tables, spectrum knots or
  * a monochromatic wavelength, one track table (sources' smear_table 0),
  * spherical targets, sources); hits go to the
  * caller's device buffer d_hits (16-byte aligned, `capacity` records) and the
@@ -345,7 +344,9 @@ PP_API int pp_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_
  * with PP_ERR_INVALID.  The first call on a device looks up the array's
  * address: make it before any stream capture.  Calls share the array, so calls
  * that overlap on the GPU race.  Runs on the current device, synchronously on
- * `stream`; returns PP_ERR_OVERFLOW when more than `capacity` hits occur. */
+ * `stream`: it copies the inputs from host memory, reads counters back and
+ * synchronises the stream, so a call cannot be recorded by stream capture.
+ * Returns PP_ERR_OVERFLOW when more than `capacity` hits occur. */
 PP_API int pp_propagate_static(const pp_medium* medium, const float* spectrum_knots,
                                int32_t n_spectrum, float mono_wavelength,
                                const float* track_quantiles, int32_t n_track,

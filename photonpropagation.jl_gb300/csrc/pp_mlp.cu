@@ -472,7 +472,6 @@ constexpr size_t kMaxInferSmem = 232448 - 256;  // 227 KB opt-in less the static
 constexpr int kEpiWarps = 16;                        // epilogue warps (4 per TMEM lane quarter)
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kInferThreads = 64 + kEpiThreads;      // producer warp, MMA warp, epilogue
-constexpr int kCluster = 2;  // CTAs sharing every weight chunk by TMA multicast
 struct InferParams {
   const float* x;
   long long n;
@@ -499,9 +498,8 @@ struct InferParams {
 // other; slot 1 runs (n_layers + 1) / 2 layers behind slot 0, so that the long
 // head epilogue of one slot overlaps a hidden layer's MMAs of the other.
 // Each slot evaluates n_rounds tiles (round r: tile (r * gridDim.x +
-// blockIdx.x) * 2 + slot); every CTA runs the same number of rounds (the
-// CTAs of a cluster consume one shared weight stream), and tiles past the
-// last row are evaluated on zero rows and not stored.
+// blockIdx.x) * 2 + slot); every CTA runs the same number of rounds, and
+// tiles past the last row are evaluated on zero rows and not stored.
 struct JobIter {
   int step = -1, slot = 0, layer = 0, round = 0;
   __device__ int tile() const { return (round * (int)gridDim.x + (int)blockIdx.x) * 2 + slot; }
@@ -521,16 +519,6 @@ struct JobIter {
     }
   }
 };
-
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
-                   : "memory");
-}
 
 // Input unit u of a tile: row u % 128, features 8 (u / 128) .. + 7 (zero
 // beyond n_in and past the last row).
@@ -637,7 +625,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   if (threadIdx.x == 32) {
     for (int i = 0; i < kRingSlots; ++i) {
       pptc::mbar_init(&w_full[i], 1);
-      pptc::mbar_init(&w_empty[i], kCluster);  // released by the MMAs of every CTA
+      pptc::mbar_init(&w_empty[i], 1);  // released by the commit of the chunk's MMAs
     }
     for (int i = 0; i < 2; ++i) {
       pptc::mbar_init(&acc_full[i], 1);
@@ -648,7 +636,6 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   }
   pptc::fence_before_sync();
   __syncthreads();
-  cluster_sync();  // the peer's barriers are initialised before any copy or commit targets them
   pptc::fence_after_sync();
   const uint32_t tmem = tmem_slot;
   bool ok = true;
@@ -656,7 +643,6 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   if (warp == 0) {
     // ---------------- weight producer
     if (lane == 0) {
-      const uint32_t rank = cluster_rank();
       JobIter it;
       bool more = it.next(p);
       uint32_t k = 0;  // chunks of the shared stream seen
@@ -670,27 +656,25 @@ __global__ void __launch_bounds__(kInferThreads, 1)
             ok = false;
             break;
           }
-          // every CTA expects each chunk; one CTA of the cluster fetches it
-          // for all (chunk k from CTA rank k % kCluster)
+          // each CTA fetches its own copy of every chunk (one bulk copy,
+          // completing on the slot's full barrier)
           const uint32_t bytes = (uint32_t)rows * chunk_width(K, j) * 2u;
           asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
                            pptc::smem_u32(&w_full[slot])),
                        "r"(bytes)
                        : "memory");
-          if (k % kCluster == rank) {
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::"
-                "cluster [%0], [%1], %2, [%3], %4;" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
-                "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
-                "r"(pptc::smem_u32(&w_full[slot])), "h"((uint16_t)((1u << kCluster) - 1u))
-                : "memory");
-          }
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+              "[%3];" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
+              "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
+              "r"(pptc::smem_u32(&w_full[slot]))
+              : "memory");
         }
         more = it.next(p);
       }
       if (!ok) abort_flag = 1;
-      // every slot is released by all CTAs (their commits have landed here)
-      // and every copy has landed before shared memory is given up
+      // every slot is released (its commit has landed) and every copy has
+      // landed before shared memory is given up
       for (uint32_t q = k > kRingSlots ? k - kRingSlots : 0; q < k; ++q) {
         pptc::mbar_wait(&w_full[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
         pptc::mbar_wait(&w_empty[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
@@ -746,8 +730,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
               pptc::mma_f16(d, a_j + (uint64_t)(s * 16), b + (uint64_t)(s * 16), idesc,
                             j > 0 || s > 0);
           }
-          // the slot is free (in every CTA's view) once these MMAs complete
-          pptc::mma_commit_multicast(&w_empty[slot], (uint16_t)((1u << kCluster) - 1u));
+          // the slot is free once these MMAs complete
+          pptc::mma_commit(&w_empty[slot]);
           if (++slot == kRingSlots) {
             slot = 0;
             phase ^= 1u;
@@ -1021,7 +1005,6 @@ __global__ void __launch_bounds__(kInferThreads, 1)
   }
   pptc::fence_before_sync();
   __syncthreads();
-  cluster_sync();  // no copy or commit of the peer targets this CTA any more
   if (warp == 0) pptc::tmem_dealloc(tmem, 2 * p.slot_cols);
   if (threadIdx.x == 0 && (abort_flag || !ok)) atomicOr(p.err, 1u);
 }
@@ -1083,7 +1066,7 @@ struct pp_mlp {
   std::vector<long long> wpack_off;     // bytes per layer
   bool pack_dirty = true;
   int num_sms = 0;
-  int infer_clusters = 0;  // co-resident clusters of the inference kernel
+  int infer_ctas = 0;      // co-resident CTAs of the inference kernel
   size_t infer_smem = 0;
   long long step = 0;
   float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f, time_weight = 1.0f;
@@ -1615,31 +1598,21 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
     e = cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device);
     if (e != cudaSuccess) return cuda_fail(e, "SM count");
   }
+  if (m->infer_ctas == 0 || m->infer_smem != smem) {
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel, kInferThreads, smem);
+    if (e != cudaSuccess) return cuda_fail(e, "inference occupancy");
+    if (per_sm < 1) return fail(PP_ERR_CUDA, "inference kernel: no CTA fits an SM");
+    m->infer_ctas = per_sm * m->num_sms;
+    m->infer_smem = smem;
+  }
+  // co-resident CTAs, each with two tiles per round
+  const long long grid = std::min<long long>(m->infer_ctas, (tiles + 1) / 2);
+  p.n_rounds = (int)((tiles + 2 * grid - 1) / (2 * grid));
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kCluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(kInferThreads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  if (m->infer_clusters == 0 || m->infer_smem != smem) {
-    cfg.gridDim = dim3((unsigned)(kCluster * ((m->num_sms + kCluster - 1) / kCluster)));
-    int nc = 0;
-    e = cudaOccupancyMaxActiveClusters(&nc, infer_kernel, &cfg);
-    if (e != cudaSuccess) return cuda_fail(e, "cluster occupancy");
-    if (nc < 1) return fail(PP_ERR_CUDA, "inference kernel: no cluster fits an SM pair");
-    m->infer_clusters = nc;
-    m->infer_smem = smem;
-  }
-  // clusters co-resident at once, each with two tiles per CTA per round
-  const long long clusters =
-      std::min<long long>(m->infer_clusters, (tiles + 2 * kCluster - 1) / (2 * kCluster));
-  const long long grid = clusters * kCluster;
-  p.n_rounds = (int)((tiles + 2 * grid - 1) / (2 * grid));
   cfg.gridDim = dim3((unsigned)grid);
   e = cudaLaunchKernelEx(&cfg, infer_kernel, p);
   if (e != cudaSuccess) return cuda_fail(e, "infer kernel");

@@ -2,9 +2,9 @@
 //
 // Some callers cannot call cudaMalloc: code that runs while another framework
 // owns the device memory through its own pooling allocator (a Julia CUDA.jl
-// memory pool, a caching allocator that must see every allocation), code that
-// is being recorded into a larger CUDA graph by its caller, or services that
-// forbid allocation after start-up so that memory use stays fixed.  For them
+// memory pool, a caching allocator that must see every allocation), or
+// services that forbid allocation after start-up so that memory use stays
+// fixed.  For them
 // pp_propagate_static runs the propagation with every piece of scratch memory
 // (device copies of the tables, the culling grid and its build buffers, the
 // safety field, the work queue and the counters) carved out of one
@@ -17,6 +17,9 @@
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress, once per device, with that device current); make
 //     that first call before any stream capture begins;
+//   * every call copies its inputs from host memory, reads the grid totals
+//     and the counters back to the host and synchronises `stream` before it
+//     returns, so a call cannot itself be recorded by stream capture;
 //   * every call shares the one array and keeps the last call's contents, so
 //     calls that overlap on the GPU (several host threads or streams at once)
 //     race: serialise them;
@@ -228,8 +231,10 @@ extern "C" PP_API int pp_propagate_static(
   if (rc != PP_OK) return rc;
   cudaStream_t stream = (cudaStream_t)stream_ptr;
   int dev = 0, num_sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t ae = cudaGetDevice(&dev);
+  if (ae == cudaSuccess) ae = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (ae != cudaSuccess) return cuda_fail(ae, "SM count");
+  if (num_sms < 1) return fail(PP_ERR_CUDA, "device reports no multiprocessors");
 
   // ---- host-side shapes and the work queue ----
   pp::GridDev gshape;

@@ -28,7 +28,7 @@ def _columns(path):
     return {k: [float(r[k]) for r in rows] for k in rows[0]}
 
 
-def main(root="/root/reference"):
+def main(root):
     assets = os.path.join(root, "assets")
     with open(os.path.join(assets, "as.set50_p0=-0.27_p1=-0.042")) as f:
         values = [float(line) for line in f if line.strip()]
@@ -52,4 +52,7 @@ def main(root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PP_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: %s <reference checkout> (or set PP_REFERENCE_ROOT)" % sys.argv[0])
+    main(root)

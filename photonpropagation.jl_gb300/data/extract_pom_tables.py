@@ -188,4 +188,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PP_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: %s <reference checkout> (or set PP_REFERENCE_ROOT)" % sys.argv[0])
+    main(root)

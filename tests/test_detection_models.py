@@ -9,6 +9,8 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# the reference checkout whose asset tables the committed CSVs are extracted from
+REF_ROOT = os.environ.get("PP_REFERENCE_ROOT", "")
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pmt_oracle  # noqa: E402
 
@@ -57,14 +59,15 @@ def test_tables(pp):
     assert f[0, 1] == 1.0 and f[-1, 1] == -1.0
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/assets"), reason="reference assets absent")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "assets")),
+                    reason="set PP_REFERENCE_ROOT to a reference checkout with its assets")
 def test_tables_extracted_from_reference(tmp_path, monkeypatch):
     """The committed CSVs are what the extraction script makes from the
     reference's assets."""
     sys.path.insert(0, os.path.join(ROOT, "photonpropagation.jl_gb300", "data"))
     import extract_detection_tables as ex
     monkeypatch.setattr(ex, "HERE", str(tmp_path))
-    ex.main("/root/reference")
+    ex.main(REF_ROOT)
     data = os.path.join(ROOT, "photonpropagation.jl_gb300", "data")
     for f in ("dom_angular_acceptance.csv", "dom_wl_acceptance.csv", "multipmt_qe.csv"):
         assert open(tmp_path / f).read() == open(os.path.join(data, f)).read(), f

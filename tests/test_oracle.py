@@ -126,6 +126,35 @@ def test_cascadia_medium_two_restatements_agree(orc, pp):
         np.testing.assert_allclose(list(out32), want, rtol=2e-6)
 
 
+def test_medium_pinned_to_reference_printout(orc, pp):
+    """The one medium value the reference itself prints.  examples/axicone.ipynb
+    (cell 2) builds the Cascadia medium with g = 0.99 and unit scales and
+    prints, at 488 nm, "Absorpion length: 26.775087" and "Scattering length:
+    56.86782" (Float32 shortest form).  Neither length depends on g or on the
+    pure-water fraction, so CascadiaMediumProperties(0.99, 0.2, 1, 1) must give
+    the same two Float32 values in every form that feeds the kernel: the FP64
+    host restatement, the oracle's FP32 and FP64 evaluations, and the knot of
+    the device table (488 nm falls exactly on a 0.125 nm knot, where the
+    kernel's linear interpolation returns the knot itself)."""
+    want_abs, want_sca = np.float32(26.775087), np.float32(56.86782)
+    med = pp.CascadiaMediumProperties(0.99, 0.2, 1.0, 1.0)
+    assert np.float32(med.absorption_length(488.0)) == want_abs
+    assert np.float32(med.scattering_length(488.0)) == want_sca
+    L = orc.load()
+    m, keep = orc.make_medium(med.oracle_params())
+    out = (ctypes.c_double * 4)()
+    out32 = (ctypes.c_float * 4)()
+    L.ppo_medium_eval_f64(ctypes.byref(m), 488.0, out)
+    L.ppo_medium_eval_f32(ctypes.byref(m), 488.0, out32)
+    assert (np.float32(out[0]), np.float32(out[2])) == (want_sca, want_abs)
+    assert (np.float32(out32[0]), np.float32(out32[2])) == (want_sca, want_abs)
+    t = med.tables(300.0, 800.0)
+    x = (np.float32(488.0) - np.float32(t.wl_min)) * np.float32(1.0 / t.wl_step)
+    i = int(x)
+    assert float(x) == i  # a knot: the interpolation weight is exactly 0
+    assert (t.scattering_length[i], t.absorption_length[i]) == (want_sca, want_abs)
+
+
 def test_cascadia_values_and_reference_constants(pp):
     med = pp.CascadiaMediumProperties()
     # MixedHGES(0.95, 0.835, 1 - 0.2) and the README's one-argument form

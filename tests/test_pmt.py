@@ -8,6 +8,8 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# the reference checkout whose asset tables the committed CSVs are extracted from
+REF_ROOT = os.environ.get("PP_REFERENCE_ROOT", "")
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pmt_oracle  # noqa: E402
 
@@ -51,14 +53,15 @@ def test_pom_tables_and_geometry(pp):
     np.testing.assert_allclose(pom.pom_pmt_directions(R), d @ R.T, atol=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/assets"), reason="reference assets absent")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "assets")),
+                    reason="set PP_REFERENCE_ROOT to a reference checkout with its assets")
 def test_pom_tables_extracted_from_reference(pp, tmp_path, monkeypatch):
     """The committed CSVs are what the extraction script makes from the
     reference's assets."""
     sys.path.insert(0, os.path.join(ROOT, "photonpropagation.jl_gb300", "data"))
     import extract_pom_tables as ex
     monkeypatch.setattr(ex, "HERE", str(tmp_path))
-    ex.main("/root/reference")
+    ex.main(REF_ROOT)
     data = os.path.join(ROOT, "photonpropagation.jl_gb300", "data")
     for f in ("pom_pmt_acceptance.csv", "pom_pmt_sigma.csv", "pom_rel_qe.csv"):
         assert open(tmp_path / f).read() == open(os.path.join(data, f)).read(), f

@@ -1,8 +1,8 @@
 """pp_propagate_static -- the entry point for callers that cannot call
-cudaMalloc (another framework's pool owns the device memory, the call is being
-recorded into a graph, or memory use is fixed at start-up).  It must give the
-same hits as the context-based pp_propagate, twice in a row, while taking all
-of its scratch from the library's static device array.
+cudaMalloc (another framework's pool owns the device memory, or memory use is
+fixed at start-up).  It must give the same hits as the context-based
+pp_propagate, twice in a row, while taking all of its scratch from the
+library's static device array, and leave the device's free memory unchanged.
 
 Collected last on purpose: if it fails, a run that stops at the first
 failure has already run every other test."""
@@ -88,8 +88,13 @@ def test_static_scratch_matches_context_entry_point(pp, gpu_ctx, which):
     raw = torch.empty(capacity * 80, dtype=torch.uint8, device="cuda")
     for call in range(2):  # two calls in a row share the static array
         raw.fill_(0xff)
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc, ctr = _static_call(pp, setup, raw.data_ptr(), capacity)
+        free_after = torch.cuda.mem_get_info()[0]
         assert rc == 0, pp._lib.last_error()
+        if call == 1:  # the first call may load the module's image; later ones allocate nothing
+            assert free_after == free_before, (free_before, free_after)
         assert ctr.n_hits == n_ref and ctr.n_ph_sim == sim_ref and ctr.err_flags == 0
         got = _sorted(_records_to_columns(pp, raw.cpu().numpy(), int(ctr.n_hits)))
         for k in FIELDS:
