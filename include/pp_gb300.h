@@ -127,7 +127,7 @@ typedef struct pp_medium {
 
 /* Launch tuning (chosen by pp_autotune or set by the caller). */
 typedef struct pp_tuning {
-  int32_t block_threads;      /* CTA size, multiple of 32, 64..512           */
+  int32_t block_threads;      /* CTA size, multiple of 32, 64..1024          */
   int32_t photons_per_thread; /* photons each lane takes per queued chunk    */
   int32_t ctas_per_sm;        /* 0 = occupancy maximum                       */
   int32_t precise_math;       /* 1 = IEEE libm functions (replay checks)     */

@@ -154,7 +154,7 @@ struct pp_ctx {
   bool has_sources = false;
   bool needs_track = false;
 
-  pp_tuning tuning{512, 8, 0, 0, 0.0f, 0, 0.0f, 0};
+  pp_tuning tuning{1024, 8, 0, 0, 0.0f, 0, 0.0f, 0};
 
   // scratch of pp_propagate
   pp_hit_record* d_hits = nullptr;
@@ -265,7 +265,7 @@ bool use_smem_grid(const pp_ctx* ctx) {
   if (ctx->tuning.grid_in_global) return false;
   return pp::propagate_smem_bytes(ctx->grid.blob_bytes, ctx->sgrid.bytes, true,
                                   ctx->tuning.block_threads, nullptr, nullptr) <=
-         pp::kSmemPerCtaBudget;
+         pp::smem_budget(ctx->tuning.block_threads);
 }
 
 LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_record* hits,
@@ -643,8 +643,8 @@ PP_API int pp_set_sources(pp_ctx* ctx, const pp_source* s, int32_t n, float phot
 PP_API int pp_set_tuning(pp_ctx* ctx, const pp_tuning* t) {
   wait_launches(ctx);  // inputs of launches in flight are about to change
   if (!ctx || !t) return set_error(PP_ERR_INVALID, "null argument");
-  if (t->block_threads < 64 || t->block_threads > 512 || (t->block_threads % 32) != 0)
-    return set_error(PP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 512]");
+  if (t->block_threads < 64 || t->block_threads > 1024 || (t->block_threads % 32) != 0)
+    return set_error(PP_ERR_INVALID, "block_threads must be a multiple of 32 in [64, 1024]");
   if (t->safety_cell < 0.0f) return set_error(PP_ERR_INVALID, "safety_cell must be >= 0");
   if (t->photons_per_thread < 1 || t->photons_per_thread > 4096)
     return set_error(PP_ERR_INVALID, "photons_per_thread must be in [1, 4096]");
@@ -953,11 +953,11 @@ PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sampl
   };
 
   // Stage 1: grid cell size, then stage 2: safety-field cell size, both at a
-  // 512-thread launch; stage 3: launch shape at the chosen sizes.
+  // 1024-thread launch; stage 3: launch shape at the chosen sizes.
   const float auto_h = ctx->grid.cell[0];
   const float auto_s = ctx->sgrid.cell;
   pp_tuning best = orig_tuning;
-  best.block_threads = 512;
+  best.block_threads = 1024;
   double best_ms = 1e300;
   if (!ctx->h_targets.empty()) {
     const float cell_factors[] = {0.75f, 1.0f, 1.5f, 2.0f};
@@ -1000,7 +1000,7 @@ PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sampl
     }
   }
   best_ms = 1e300;
-  const int blocks[] = {256, 512};
+  const int blocks[] = {512, 1024};
   const int ppts[] = {2, 8};
   for (int b : blocks) {
     for (int p : ppts) {

@@ -312,14 +312,16 @@ __device__ __forceinline__ bool shape_hit(const float4* __restrict__ shapes, int
 
 // First target in index order intersected within (0, step): the candidates
 // come from a 3-D DDA walk over the uniform grid cells the segment crosses
-// (Amanatides & Woo); among all intersected candidates the smallest index
+// between t_lo and t_hi (0 <= t_lo, t_hi <= step: the part of the segment
+// that may come near a target; the sphere test itself always uses the whole
+// segment) (Amanatides & Woo); among all intersected candidates the smallest index
 // wins, which is exactly the reference's "first target in index order"
 // (src/photon_prop_cuda.jl:497-506).  Returns the 0-based index or -1.
 template <bool P>
 __device__ __forceinline__ int first_hit(const pp::GridDev& g, const uint32_t* __restrict__ cells,
                                          const uint16_t* __restrict__ items,
                                          const float4* __restrict__ sph, float3 pos, float3 dir,
-                                         float step, float* d_out) {
+                                         float step, float t_lo, float t_hi, float* d_out) {
   // Reciprocal direction; zero components become a huge value of the same
   // sign as the step direction chosen below (+ for +0 and -0 alike).
   const float ix = approx_rcp(fabsf(dir.x) > 1e-20f ? dir.x : 1e-20f);
@@ -329,8 +331,8 @@ __device__ __forceinline__ int first_hit(const pp::GridDev& g, const uint32_t* _
   const float tx0 = (g.lo[0] - pos.x) * ix, tx1 = (g.hi[0] - pos.x) * ix;
   const float ty0 = (g.lo[1] - pos.y) * iy, ty1 = (g.hi[1] - pos.y) * iy;
   const float tz0 = (g.lo[2] - pos.z) * iz, tz1 = (g.hi[2] - pos.z) * iz;
-  const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
-  const float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), step));
+  const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), t_lo));
+  const float tmax = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), t_hi));
   if (!(tmin <= tmax)) return -1;
 
   const int nx = g.dims[0], ny = g.dims[1], nz = g.dims[2];

@@ -50,14 +50,19 @@ constexpr float kSafetyQuantum = 0.5f;  // m per uint8 step (saturates at 127.5 
 
 // Per-warp shared-memory state of the propagation kernel: the queue of
 // deferred step segments and, per lane, the earliest hit found so far.
-constexpr int kQueueCap = 32;
-constexpr int kMaxBlockThreads = 512;
+// Entries [0, checked) of the queue have been clipped by the safety field and
+// wait for the grid walk over [t0, t1]; entries from `checked` on wait to be
+// clipped (at most 32 of them at a time).
+constexpr int kQueueCap = 64;
+constexpr int kMaxBlockThreads = 1024;
 struct WarpQueue {
   float px[kQueueCap], py[kQueueCap], pz[kQueueCap];
   float dx[kQueueCap], dy[kQueueCap], dz[kQueueCap];
   float len[kQueueCap];
   float dist0[kQueueCap];     // compensated path length at the segment start
   uint32_t meta[kQueueCap];   // owner lane | step << 8
+  float t0[kQueueCap];        // part of the segment the grid walk must cover
+  float t1[kQueueCap];
 };
 struct WarpBest {
   uint32_t key[32];           // step << 16 | target index; ~0 = none
@@ -191,8 +196,15 @@ inline size_t propagate_smem_bytes(uint32_t blob_bytes, uint32_t safety_bytes, b
   if (state_offset) *state_offset = (uint32_t)off;
   return off + (size_t)(block_threads / 32) * (sizeof(WarpQueue) + sizeof(WarpBest));
 }
-// Largest dynamic shared memory per CTA for which two CTAs fit on an SM.
-constexpr size_t kSmemPerCtaBudget = 110 * 1024;
+// Largest dynamic shared memory per CTA for which CTAs of block_threads
+// still fill an SM with 1024 threads (the 64-register cap of the kernel): the
+// SM's 228 KB less 1 KB reserved per CTA and the static barrier, at most the
+// 227 KB one CTA may opt into.
+inline size_t smem_budget(int block_threads) {
+  const int ctas = block_threads >= 1024 ? 1 : 1024 / (block_threads > 0 ? block_threads : 1);
+  const size_t b = (size_t)228 * 1024 / (size_t)ctas - 1024 - 64;
+  return b < (size_t)227 * 1024 - 64 ? b : (size_t)227 * 1024 - 64;
+}
 
 // Host-side launch of the propagation kernel (pp_propagate.cu).
 cudaError_t launch_propagate(const LaunchArgs& args, int block_threads, int ctas_per_sm,

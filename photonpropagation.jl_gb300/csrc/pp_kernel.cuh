@@ -17,13 +17,16 @@
 //   * speculative stepping with deferred hit tests.  Each lane runs all
 //     n_steps of its photon without waiting for the target test.  A step
 //     segment is cleared cheaply when the safety field proves that no target
-//     lies within the ball around its midpoint (or the two balls around its
-//     quarter points); the rare uncleared segments go to a per-warp queue in
-//     shared memory that the warp drains densely, one segment per lane,
-//     through the uniform-grid DDA.  The photon's hit is the earliest step
-//     with an intersection and, within it, the lowest target index -- the
-//     reference's "first target in index order" (:497-506).  Steps after the
-//     hit were computed speculatively and are discarded;
+//     lies within the ball around its midpoint; the rare uncleared segments
+//     go to a per-warp queue in shared memory.  When 32 of them wait, the warp
+//     clips them, one per lane, by sphere tracing the safety field from both
+//     ends (most vanish); the survivors stay queued with the part of the
+//     segment that may come near a target, and whenever 32 survivors wait the
+//     warp walks them, one per lane, through the uniform-grid DDA over that
+//     part only.  The photon's hit is the earliest step with an intersection
+//     and, within it, the lowest target index -- the reference's "first
+//     target in index order" (:497-506).  Steps after the hit were computed
+//     speculatively and are discarded;
 //   * the target grid (cells, candidate lists, spheres) is staged once per CTA
 //     into shared memory with a TMA bulk copy completing on an mbarrier, waited
 //     on with a time bound;
@@ -141,44 +144,120 @@ __device__ __forceinline__ bool segment_clear(const SafetyDev& s, const unsigned
       h * 1.0001f + 1e-4f);
 }
 
-// Drain the warp's deferred segments: lane e tests queue entry base + e with
-// the grid DDA; the earliest (step, target) per owner lane wins via a shared
-// atomicMin on the key (step << 16 | target), and the winning lane writes
-// the hit state into the owner's slot.
-template <bool P>
-__device__ __forceinline__ void drain_queue(WarpQueue& q, WarpBest& b, int count,
-                                            const GridDev& g, const uint32_t* cells,
-                                            const uint16_t* items, const float4* sph, int lane) {
-  for (int base = 0; base < count; base += 32) {
-    const int e = base + lane;
-    int j = -1, owner = 0;
-    uint32_t key = 0;
-    float d = 0.0f, d0 = 0.0f;
-    float3 p = make_float3(0.0f, 0.0f, 0.0f), dir = p;
-    if (e < count) {
-      p = make_float3(q.px[e], q.py[e], q.pz[e]);
-      dir = make_float3(q.dx[e], q.dy[e], q.dz[e]);
-      d0 = q.dist0[e];
-      const uint32_t meta = q.meta[e];
-      owner = (int)(meta & 31u);
-      j = first_hit<P>(g, cells, items, sph, p, dir, q.len[e], &d);
-      if (j >= 0) {
-        key = ((meta >> 8) << 16) | (uint32_t)j;
-        atomicMin(&b.key[owner], key);
-      }
-    }
-    __syncwarp();
-    if (j >= 0 && b.key[owner] == key) {
-      b.hx[owner] = madd<P>(dir.x, d, p.x);
-      b.hy[owner] = madd<P>(dir.y, d, p.y);
-      b.hz[owner] = madd<P>(dir.z, d, p.z);
-      b.ox[owner] = dir.x;
-      b.oy[owner] = dir.y;
-      b.oz[owner] = dir.z;
-      b.dist[owner] = d0 + d;
-    }
-    __syncwarp();
+// Lower bound on the distance from m to every (inflated) target sphere:
+// D(c) - |m - c| for the field cell c nearest to m (distance is 1-Lipschitz,
+// D(c) is stored quantised down).  Valid for any m; weak (often negative) far
+// outside the field's box.
+template <bool kShared, bool P>
+__device__ __forceinline__ float field_bound(const SafetyDev& s, const unsigned char* __restrict__ f,
+                                             float3 m) {
+  const float fx = fminf(fmaxf(floorf((m.x - s.lo[0]) * s.inv_cell), 0.0f), (float)(s.dims[0] - 1));
+  const float fy = fminf(fmaxf(floorf((m.y - s.lo[1]) * s.inv_cell), 0.0f), (float)(s.dims[1] - 1));
+  const float fz = fminf(fmaxf(floorf((m.z - s.lo[2]) * s.inv_cell), 0.0f), (float)(s.dims[2] - 1));
+  const int idx = (int)fmaf(fmaf(fz, (float)s.dims[1], fy), (float)s.dims[0], fx);
+  const float D = (float)(kShared ? f[idx] : __ldg(f + idx)) * kSafetyQuantum;
+  const float ox = fmaf(fx + 0.5f, s.cell, s.lo[0]) - m.x;
+  const float oy = fmaf(fy + 0.5f, s.cell, s.lo[1]) - m.y;
+  const float oz = fmaf(fz + 0.5f, s.cell, s.lo[2]) - m.z;
+  return D - f_sqrt<P>(ox * ox + oy * oy + oz * oz);
+}
+
+// Slack (m) taken off each clipped end: covers the rounding of the traced
+// points and of the square root, well inside the 1 cm by which the field's
+// spheres are inflated.
+constexpr float kClipSlack = 5e-3f;
+
+// Clip the unchecked queue entries [n2, n2 + n1) (n1 <= 32, one per lane) by
+// sphere tracing the safety field twice from each end: no target lies within
+// field_bound(p) of a point p, so the walk can skip [0, t0) and (t1, L].
+// Entries left with t0 < t1 are compacted (in place) to [n2, n2 + kept) with
+// their interval; the others cannot hit anything and are dropped.  Returns
+// the new number of checked entries.
+template <bool kShared, bool P>
+__device__ __forceinline__ int check_queue(WarpQueue& q, int n2, int n1, const SafetyDev& s,
+                                           const unsigned char* __restrict__ f, int lane) {
+  const int src = n2 + lane;
+  bool keep = false;
+  float3 p = make_float3(0.0f, 0.0f, 0.0f), d = p;
+  float L = 0.0f, d0 = 0.0f, t0 = 0.0f, t1 = 0.0f;
+  uint32_t meta = 0;
+  if (lane < n1) {
+    p = make_float3(q.px[src], q.py[src], q.pz[src]);
+    d = make_float3(q.dx[src], q.dy[src], q.dz[src]);
+    L = q.len[src];
+    t0 = fmaxf(field_bound<kShared, P>(s, f, p), 0.0f);
+    t0 += fmaxf(field_bound<kShared, P>(
+                    s, f, make_float3(fmaf(d.x, t0, p.x), fmaf(d.y, t0, p.y), fmaf(d.z, t0, p.z))),
+                0.0f);
+    t1 = L - fmaxf(field_bound<kShared, P>(
+                       s, f, make_float3(fmaf(d.x, L, p.x), fmaf(d.y, L, p.y), fmaf(d.z, L, p.z))),
+                   0.0f);
+    t1 -= fmaxf(field_bound<kShared, P>(
+                    s, f, make_float3(fmaf(d.x, t1, p.x), fmaf(d.y, t1, p.y), fmaf(d.z, t1, p.z))),
+                0.0f);
+    t0 = fmaxf(t0 - kClipSlack, 0.0f);
+    t1 = fminf(t1 + kClipSlack, L);
+    keep = t0 < t1;
+    d0 = q.dist0[src];
+    meta = q.meta[src];
   }
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  __syncwarp();  // every entry is read before any is overwritten
+  if (keep) {
+    const int dst = n2 + __popc(m & ((1u << lane) - 1u));
+    q.px[dst] = p.x;
+    q.py[dst] = p.y;
+    q.pz[dst] = p.z;
+    q.dx[dst] = d.x;
+    q.dy[dst] = d.y;
+    q.dz[dst] = d.z;
+    q.len[dst] = L;
+    q.dist0[dst] = d0;
+    q.meta[dst] = meta;
+    q.t0[dst] = t0;
+    q.t1[dst] = t1;
+  }
+  __syncwarp();
+  return n2 + __popc(m);
+}
+
+// Test the checked entries [base, base + c) (c <= 32): lane e walks entry
+// base + e through the grid DDA over its clipped interval; the earliest
+// (step, target) per owner lane wins via a shared atomicMin on the key
+// (step << 16 | target), and the winning lane writes the hit state into the
+// owner's slot.
+template <bool P>
+__device__ __forceinline__ void test_queue(WarpQueue& q, WarpBest& b, int base, int c,
+                                           const GridDev& g, const uint32_t* cells,
+                                           const uint16_t* items, const float4* sph, int lane) {
+  const int e = base + lane;
+  int j = -1, owner = 0;
+  uint32_t key = 0;
+  float d = 0.0f, d0 = 0.0f;
+  float3 p = make_float3(0.0f, 0.0f, 0.0f), dir = p;
+  if (lane < c) {
+    p = make_float3(q.px[e], q.py[e], q.pz[e]);
+    dir = make_float3(q.dx[e], q.dy[e], q.dz[e]);
+    d0 = q.dist0[e];
+    const uint32_t meta = q.meta[e];
+    owner = (int)(meta & 31u);
+    j = first_hit<P>(g, cells, items, sph, p, dir, q.len[e], q.t0[e], q.t1[e], &d);
+    if (j >= 0) {
+      key = ((meta >> 8) << 16) | (uint32_t)j;
+      atomicMin(&b.key[owner], key);
+    }
+  }
+  __syncwarp();
+  if (j >= 0 && b.key[owner] == key) {
+    b.hx[owner] = madd<P>(dir.x, d, p.x);
+    b.hy[owner] = madd<P>(dir.y, d, p.y);
+    b.hz[owner] = madd<P>(dir.z, d, p.z);
+    b.ox[owner] = dir.x;
+    b.oy[owner] = dir.y;
+    b.oz[owner] = dir.z;
+    b.dist[owner] = d0 + d;
+  }
+  __syncwarp();
 }
 
 // Append one hit: one atomic per warp for all lanes that record in this pass.
@@ -208,9 +287,9 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
   }
 }
 
-// Two CTAs of kMaxBlockThreads per SM caps the kernel at 64 registers.
+// One CTA of kMaxBlockThreads per SM caps the kernel at 64 registers.
 #ifndef PP_PROPAGATE_MIN_BLOCKS
-#define PP_PROPAGATE_MIN_BLOCKS 2
+#define PP_PROPAGATE_MIN_BLOCKS 1
 #endif
 
 // kShapes: shaped targets (a.shapes), every target tested at every step in
@@ -361,7 +440,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
       float dist = 0.0f, comp = 0.0f;  // Kahan-compensated path length
       best.key[lane] = 0xffffffffu;
       __syncwarp();
-      int count = 0;  // warp-uniform length of the deferred-segment queue
+      // warp-uniform queue state: [0, n2) clipped, [n2, n2 + n1) not yet
+      int n1 = 0, n2 = 0;
       bool found = false;  // shaped targets: the photon has hit
       for (int k = 1; k <= a.n_steps; ++k) {
         const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.round_keys);
@@ -414,12 +494,17 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         const unsigned m = __ballot_sync(0xffffffffu, need);
         if (m) {
           const int nn = __popc(m);
-          if (count + nn > kQueueCap) {
-            drain_queue<kPrecise>(q, best, count, a.grid, cells, items, sph, lane);
-            count = 0;
+          if (n1 + nn > 32) {
+            // clip the unchecked entries; walk the grid once 32 checked ones wait
+            n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.sgrid, field, lane);
+            n1 = 0;
+            if (n2 >= 32) {
+              n2 -= 32;
+              test_queue<kPrecise>(q, best, n2, 32, a.grid, cells, items, sph, lane);
+            }
           }
           if (need) {
-            const int e = count + __popc(m & lanemask_lt);
+            const int e = n2 + n1 + __popc(m & lanemask_lt);
             q.px[e] = pos.x;
             q.py[e] = pos.y;
             q.pz[e] = pos.z;
@@ -430,7 +515,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
             q.dist0[e] = dist - comp;
             q.meta[e] = (uint32_t)lane | ((uint32_t)k << 8);
           }
-          count += nn;
+          n1 += nn;
           __syncwarp();
         }
         }  // kShapes
@@ -443,8 +528,14 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         }
         dir = update_direction<kPrecise>(a.phase, dir, u01(r.y), u01(r.z), u01(r.w));
       }
-      if (!kShapes && count > 0)
-        drain_queue<kPrecise>(q, best, count, a.grid, cells, items, sph, lane);
+      if (!kShapes) {
+        if (n1 > 0) n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.sgrid, field, lane);
+        while (n2 > 0) {
+          const int c = n2 < 32 ? n2 : 32;
+          n2 -= c;
+          test_queue<kPrecise>(q, best, n2, c, a.grid, cells, items, sph, lane);
+        }
+      }
       __syncwarp();
 
       const uint32_t key = best.key[lane];

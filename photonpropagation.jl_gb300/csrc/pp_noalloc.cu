@@ -241,7 +241,7 @@ extern "C" PP_API int pp_propagate_static(
   grid_shape(targets, n_targets, cell_size, &gshape);
   pp::SafetyDev sshape;
   safety_shape(gshape, &sshape);
-  const int ppt = 8, block = 512;
+  const int ppt = 8, block = 1024;
   const long long chunk = 32LL * ppt;
   std::vector<unsigned long long> prefix(n_src + 1, 0);
   std::vector<long long> nph(std::max(n_src, 1), 0);
@@ -336,7 +336,7 @@ extern "C" PP_API int pp_propagate_static(
   a.wait_limit_ns = 2000000000ull;
   if (a.total_chunks > 0) {
     const bool smem = pp::propagate_smem_bytes(grid.blob_bytes, sshape.bytes, true, block, nullptr,
-                                               nullptr) <= pp::kSmemPerCtaBudget;
+                                               nullptr) <= pp::smem_budget(block);
     e = pp::launch_propagate(a, block, 0, false, smem, num_sms, stream, nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "launch propagate kernel");
   }

@@ -332,7 +332,7 @@ def test_public_autotune_keeps_results(pp, gpu_ctx):
     orig = gpu_ctx.get_tuning()
     try:
         t = pp.autotune(setup, 15, sample_photons=1_000_000)
-        assert 64 <= t["block_threads"] <= 512 and t["block_threads"] % 32 == 0
+        assert 64 <= t["block_threads"] <= 1024 and t["block_threads"] % 32 == 0
         assert t["photons_per_thread"] >= 1 and t["cell_size"] > 0 and t["photons_per_s"] > 0
         after = pp.propagate_photons(setup)
     finally:

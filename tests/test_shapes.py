@@ -116,7 +116,7 @@ def test_autotune_with_shaped_targets(pp, gpu_ctx):
                                   setup.photon_scaling, n)
         before = ctx.fetch_hits(nh)
         t, rate = ctx.autotune(setup.seed, 15, sample_photons=200_000)
-        assert rate > 0 and 64 <= t.block_threads <= 512
+        assert rate > 0 and 64 <= t.block_threads <= 1024
         rc2, nh2, _ = ctx.propagate(recs, len(setup.sources), setup.seed, 15,
                                     setup.photon_scaling, n)
         after = ctx.fetch_hits(nh2)
