@@ -134,7 +134,10 @@ typedef struct pp_tuning {
   float cell_size;            /* target-grid cell edge (m); 0 = automatic    */
   int32_t grid_in_global;     /* 1 = read the grid from global memory        */
   float safety_cell;          /* safety-field cell edge (m); 0 = automatic   */
-  int32_t reserved;
+  int32_t target_loop;        /* 1 = no culling: every sphere is tested at    */
+                              /* every step in index order, the reference's   */
+                              /* own loop (src/photon_prop_cuda.jl:497-506);  */
+                              /* same hits, for comparisons                   */
 } pp_tuning;
 
 /* One hit as written by the kernel into device memory: 80 bytes, 16-byte

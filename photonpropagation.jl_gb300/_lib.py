@@ -69,7 +69,7 @@ class pp_tuning(Structure):
     _fields_ = [
         ("block_threads", c_int32), ("photons_per_thread", c_int32), ("ctas_per_sm", c_int32),
         ("precise_math", c_int32), ("cell_size", c_float), ("grid_in_global", c_int32),
-        ("safety_cell", c_float), ("reserved", c_int32),
+        ("safety_cell", c_float), ("target_loop", c_int32),
     ]
 
 

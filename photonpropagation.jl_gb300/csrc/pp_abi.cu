@@ -133,6 +133,7 @@ struct pp_ctx {
   std::vector<pp_sphere> h_targets;
   pp_sphere* d_targets = nullptr;
   float4* d_shapes = nullptr;  // shaped targets (then the sphere list is empty)
+  float4* d_loop_spheres = nullptr;  // the sphere list as shape records (target_loop)
   int n_shapes = 0;
   unsigned char* d_blob = nullptr;
   GridDev grid{};
@@ -282,6 +283,10 @@ LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_reco
   a.safety = ctx->d_safety;
   a.shapes = ctx->n_shapes > 0 ? ctx->d_shapes : nullptr;
   a.n_shapes = ctx->n_shapes;
+  if (ctx->n_shapes == 0 && ctx->tuning.target_loop && !ctx->h_targets.empty()) {
+    a.shapes = ctx->d_loop_spheres;
+    a.n_shapes = (int)ctx->h_targets.size();
+  }
   a.sgrid = ctx->sgrid;
   a.medium = ctx->d_medium;
   a.n_medium = ctx->n_medium;
@@ -393,6 +398,7 @@ PP_API int pp_destroy(pp_ctx* ctx) {
   cudaFree(ctx->d_track);
   cudaFree(ctx->d_targets);
   cudaFree(ctx->d_shapes);
+  cudaFree(ctx->d_loop_spheres);
   cudaFree(ctx->d_blob);
   cudaFree(ctx->d_safety);
   cudaFree(ctx->d_sources);
@@ -516,10 +522,26 @@ PP_API int pp_set_targets(pp_ctx* ctx, const pp_sphere* t, int32_t n, float cell
   ctx->h_targets.assign(t, t + n);
   cudaFree(ctx->d_targets);
   ctx->d_targets = nullptr;
+  cudaFree(ctx->d_loop_spheres);
+  ctx->d_loop_spheres = nullptr;
   if (n > 0) {
     PP_CUDA(cudaMalloc(&ctx->d_targets, sizeof(pp_sphere) * n), "cudaMalloc(targets)");
     PP_CUDA(cudaMemcpy(ctx->d_targets, t, sizeof(pp_sphere) * n, cudaMemcpyHostToDevice),
             "upload targets");
+    // the same spheres as shape records, for the unculled loop (target_loop)
+    std::vector<float4> h(2 * (size_t)n);
+    int kind = PP_TARGET_SPHERE;
+    float kf;
+    memcpy(&kf, &kind, sizeof(kf));
+    for (int i = 0; i < n; ++i) {
+      h[2 * i] = make_float4(t[i].position[0], t[i].position[1], t[i].position[2],
+                             t[i].radius * t[i].radius);
+      h[2 * i + 1] = make_float4(0.0f, kf, 0.0f, 0.0f);
+    }
+    PP_CUDA(cudaMalloc(&ctx->d_loop_spheres, sizeof(float4) * h.size()), "cudaMalloc(loop targets)");
+    PP_CUDA(cudaMemcpy(ctx->d_loop_spheres, h.data(), sizeof(float4) * h.size(),
+                       cudaMemcpyHostToDevice),
+            "upload loop targets");
   }
   const float h = cell_size > 0.0f ? cell_size : ctx->tuning.cell_size;
   int rc = rebuild_grid(ctx, h);
@@ -649,6 +671,8 @@ PP_API int pp_set_tuning(pp_ctx* ctx, const pp_tuning* t) {
   if (t->photons_per_thread < 1 || t->photons_per_thread > 4096)
     return set_error(PP_ERR_INVALID, "photons_per_thread must be in [1, 4096]");
   if (t->ctas_per_sm < 0) return set_error(PP_ERR_INVALID, "ctas_per_sm must be >= 0");
+  if (t->target_loop != 0 && t->target_loop != 1)
+    return set_error(PP_ERR_INVALID, "target_loop must be 0 or 1");
   DeviceScope ds(ctx->device);
   const bool ppt_changed = t->photons_per_thread != ctx->tuning.photons_per_thread;
   const bool cell_changed =

@@ -167,15 +167,17 @@ __device__ __forceinline__ float field_bound(const SafetyDev& s, const unsigned 
 // spheres are inflated.
 constexpr float kClipSlack = 5e-3f;
 
-// Clip the unchecked queue entries [n2, n2 + n1) (n1 <= 32, one per lane) by
-// sphere tracing the safety field twice from each end: no target lies within
-// field_bound(p) of a point p, so the walk can skip [0, t0) and (t1, L].
-// Entries left with t0 < t1 are compacted (in place) to [n2, n2 + kept) with
-// their interval; the others cannot hit anything and are dropped.  Returns
-// the new number of checked entries.
+// Clip the unchecked queue entries [n2, n2 + n1) (n1 <= 32, one per lane):
+// first to the grid's box (no target lies outside it), then by sphere tracing
+// the safety field twice from each end of what is left -- no target lies
+// within field_bound(p) of a point p -- so the walk can skip [0, t0) and
+// (t1, L].  Entries left with t0 < t1 are compacted (in place) to
+// [n2, n2 + kept) with their interval; the others cannot hit anything and are
+// dropped.  Returns the new number of checked entries.
 template <bool kShared, bool P>
-__device__ __forceinline__ int check_queue(WarpQueue& q, int n2, int n1, const SafetyDev& s,
-                                           const unsigned char* __restrict__ f, int lane) {
+__device__ __forceinline__ int check_queue(WarpQueue& q, int n2, int n1, const GridDev& g,
+                                           const SafetyDev& s, const unsigned char* __restrict__ f,
+                                           int lane) {
   const int src = n2 + lane;
   bool keep = false;
   float3 p = make_float3(0.0f, 0.0f, 0.0f), d = p;
@@ -185,16 +187,26 @@ __device__ __forceinline__ int check_queue(WarpQueue& q, int n2, int n1, const S
     p = make_float3(q.px[src], q.py[src], q.pz[src]);
     d = make_float3(q.dx[src], q.dy[src], q.dz[src]);
     L = q.len[src];
-    t0 = fmaxf(field_bound<kShared, P>(s, f, p), 0.0f);
-    t0 += fmaxf(field_bound<kShared, P>(
-                    s, f, make_float3(fmaf(d.x, t0, p.x), fmaf(d.y, t0, p.y), fmaf(d.z, t0, p.z))),
-                0.0f);
-    t1 = L - fmaxf(field_bound<kShared, P>(
-                       s, f, make_float3(fmaf(d.x, L, p.x), fmaf(d.y, L, p.y), fmaf(d.z, L, p.z))),
-                   0.0f);
-    t1 -= fmaxf(field_bound<kShared, P>(
-                    s, f, make_float3(fmaf(d.x, t1, p.x), fmaf(d.y, t1, p.y), fmaf(d.z, t1, p.z))),
-                0.0f);
+    // slab test against the grid box (the same one the walk clips to)
+    const float ix = approx_rcp(fabsf(d.x) > 1e-20f ? d.x : 1e-20f);
+    const float iy = approx_rcp(fabsf(d.y) > 1e-20f ? d.y : 1e-20f);
+    const float iz = approx_rcp(fabsf(d.z) > 1e-20f ? d.z : 1e-20f);
+    const float tx0 = (g.lo[0] - p.x) * ix, tx1 = (g.hi[0] - p.x) * ix;
+    const float ty0 = (g.lo[1] - p.y) * iy, ty1 = (g.hi[1] - p.y) * iy;
+    const float tz0 = (g.lo[2] - p.z) * iz, tz1 = (g.hi[2] - p.z) * iz;
+    t0 = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
+    t1 = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), L));
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+      t0 += fmaxf(field_bound<kShared, P>(s, f,
+                                          make_float3(fmaf(d.x, t0, p.x), fmaf(d.y, t0, p.y),
+                                                      fmaf(d.z, t0, p.z))),
+                  0.0f);
+      t1 -= fmaxf(field_bound<kShared, P>(s, f,
+                                          make_float3(fmaf(d.x, t1, p.x), fmaf(d.y, t1, p.y),
+                                                      fmaf(d.z, t1, p.z))),
+                  0.0f);
+    }
     t0 = fmaxf(t0 - kClipSlack, 0.0f);
     t1 = fminf(t1 + kClipSlack, L);
     keep = t0 < t1;
@@ -496,7 +508,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
           const int nn = __popc(m);
           if (n1 + nn > 32) {
             // clip the unchecked entries; walk the grid once 32 checked ones wait
-            n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.sgrid, field, lane);
+            n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.grid, a.sgrid, field, lane);
             n1 = 0;
             if (n2 >= 32) {
               n2 -= 32;
@@ -529,7 +541,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         dir = update_direction<kPrecise>(a.phase, dir, u01(r.y), u01(r.z), u01(r.w));
       }
       if (!kShapes) {
-        if (n1 > 0) n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.sgrid, field, lane);
+        if (n1 > 0) n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.grid, a.sgrid, field, lane);
         while (n2 > 0) {
           const int c = n2 < 32 ? n2 : 32;
           n2 -= c;

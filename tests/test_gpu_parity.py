@@ -31,7 +31,8 @@ def gpu_run(pp, setup, n_steps=15, capacity=None, **tuning):
         ctx.set_tuning(block_threads=old.block_threads,
                        photons_per_thread=old.photons_per_thread,
                        ctas_per_sm=old.ctas_per_sm, precise_math=old.precise_math,
-                       cell_size=old.cell_size, grid_in_global=old.grid_in_global)
+                       cell_size=old.cell_size, grid_in_global=old.grid_in_global,
+                       target_loop=old.target_loop)
 
 
 def test_philox_device_matches_oracle(pp, orc, gpu_ctx):
@@ -68,10 +69,15 @@ def test_c1_detector_replay(pp, orc, gpu_ctx, precise):
 
 def test_launch_shape_and_grid_invariance(pp, gpu_ctx):
     """Per-photon random streams: the hit set does not depend on the block
-    size, photons per thread, grid cell size or where the grid is read from."""
+    size, photons per thread, grid cell size or where the grid is read from --
+    nor on the culling at all: target_loop = 1 tests every sphere at every
+    step in index order (the reference's own loop, src/photon_prop_cuda.jl:
+    497-506) and must find exactly the same hits as the culled walk."""
     setup = pp.workloads.c1_setup(photons=400_000, seed=3)
     base = None
     for tun in (dict(block_threads=256, photons_per_thread=8),
+                dict(block_threads=1024, photons_per_thread=2),
+                dict(block_threads=256, photons_per_thread=8, target_loop=1),
                 dict(block_threads=128, photons_per_thread=1),
                 dict(block_threads=512, photons_per_thread=16, grid_in_global=1),
                 dict(block_threads=256, photons_per_thread=4, cell_size=12.0),
