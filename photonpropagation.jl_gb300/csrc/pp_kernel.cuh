@@ -299,6 +299,115 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
   }
 }
 
+// Initial state of photon p of source s (initialize_photon_state,
+// src/photon_prop_cuda.jl:158-276): position, direction, emission time,
+// wavelength and the medium at that wavelength {sca_len, v_group, abs_len,
+// n}.  Deterministic in (p, s), so the step loop keeps only what it needs and
+// the few photons that hit recompute the rest when their hit is recorded.
+struct PhotonInit {
+  float3 pos, dir;
+  float t0, wl;
+  float4 med;
+};
+
+template <bool kPrecise>
+__device__ __forceinline__ PhotonInit init_photon(const LaunchArgs& a, int s, uint32_t plo,
+                                                  uint32_t phi) {
+  const pp_source* sp = a.sources + s;
+  const int kind = __ldg(&sp->kind);
+  const float3 spos = make_float3(__ldg(&sp->position[0]), __ldg(&sp->position[1]),
+                                  __ldg(&sp->position[2]));
+  const float3 saxis = make_float3(__ldg(&sp->direction[0]), __ldg(&sp->direction[1]),
+                                   __ldg(&sp->direction[2]));
+  const float stime = __ldg(&sp->time);
+  const uint4 r0 = philox(make_uint4(plo, phi, 0u, (uint32_t)s), a.round_keys);
+  const float u0 = u01(r0.x), u1 = u01(r0.y), u2 = u01(r0.z), u3 = u01(r0.w);
+  const float wl = a.spectrum ? spectrum_sample(a.spectrum, a.n_spectrum, u0)
+                              : a.mono_wavelength;
+  const float4 med = medium_at(a.medium, a.n_medium, a.med_wl_min, a.med_inv_step, wl);
+
+  // ---- initial state (initialize_photon_state) ----
+  float3 pos = spos, dir;
+  float t0 = stime;
+  switch (kind) {
+    case PP_SRC_POINTLIKE_ISOTROPIC:
+    case PP_SRC_POINTLIKE_TIME_RANGE:
+      dir = dir_from_cos<kPrecise>(uniform_ab(-1.0f, 1.0f, u1), u2);
+      if (kind == PP_SRC_POINTLIKE_TIME_RANGE)
+        t0 = uniform_ab(stime, __ldg(&sp->time_end), u3);
+      break;
+    case PP_SRC_COLLIMATED_ISOTROPIC:
+      dir = dir_from_cos<kPrecise>(uniform_ab(__ldg(&sp->cut_angle_cos), 1.0f, u2), u1);
+      break;
+    case PP_SRC_PENCIL: {
+      const float div = __ldg(&sp->beam_divergence);
+      dir = div > 0.0f ? rot_from_ez<kPrecise>(
+                             saxis, sph_to_cart<kPrecise>(
+                                        f_sqrt<kPrecise>(uniform_ab(0.0f, div * div, u1)), u2))
+                       : saxis;
+      break;
+    }
+    case PP_SRC_AXICONE: {
+      float th = __ldg(&sp->angle);
+      const float div = __ldg(&sp->beam_divergence);
+      if (div > 0.0f) {
+        float cs;
+        if (kPrecise) {
+          cs = cosf(kTwoPi * u3);
+        } else {
+          float sn;
+          f_sincos_2pi<false>(u3, &sn, &cs);
+        }
+        th += f_sqrt<kPrecise>(-2.0f * f_log<kPrecise>(u2)) * cs * div;
+      }
+      dir = rot_from_ez<kPrecise>(saxis, sph_to_cart<kPrecise>(th, u1));
+      break;
+    }
+    case PP_SRC_EXTENDED_CHERENKOV:
+    case PP_SRC_EXTENDED_CHERENKOV_NOSMEAR:
+    case PP_SRC_POINTLIKE_CHERENKOV:
+    case PP_SRC_CHERENKOV_TRACK: {
+      float along = 0.0f;
+      if (kind == PP_SRC_EXTENDED_CHERENKOV || kind == PP_SRC_EXTENDED_CHERENKOV_NOSMEAR) {
+        along = gamma_sample<kPrecise>(__ldg(&sp->long_a), 1.0f / __ldg(&sp->long_b), plo, phi,
+                                       (uint32_t)s, a.key0, a.key1) *
+                __ldg(&sp->long_lrad);
+      } else if (kind == PP_SRC_CHERENKOV_TRACK) {
+        const uint4 re = philox(make_uint4(plo, phi, kExtraCall, (uint32_t)s), a.round_keys);
+        along = uniform_ab(0.0f, __ldg(&sp->length), u01(re.x));
+      }
+      if (kind != PP_SRC_POINTLIKE_CHERENKOV) {
+        pos = make_float3(spos.x + along * saxis.x, spos.y + along * saxis.y,
+                          spos.z + along * saxis.z);
+        t0 = stime + along / kCVac;
+      }
+      dir = cherenkov_dir<kPrecise>(
+          saxis, med.w, u1, u2, u3, kind != PP_SRC_EXTENDED_CHERENKOV_NOSMEAR,
+          a.track + (size_t)__ldg(&sp->smear_table) * (size_t)a.n_track, a.n_track);
+      break;
+    }
+    default:
+      dir = make_float3(0.0f, 0.0f, 1.0f);
+      break;
+  }
+
+  PhotonInit in;
+  in.pos = pos;
+  in.dir = dir;
+  in.t0 = t0;
+  in.wl = wl;
+  in.med = med;
+  return in;
+}
+
+// The same as a call, for the hit record (rare): keeps the emission data out
+// of the step loop's registers.
+template <bool kPrecise>
+__device__ __noinline__ PhotonInit init_photon_again(const LaunchArgs& a, int s, uint32_t plo,
+                                                     uint32_t phi) {
+  return init_photon<kPrecise>(a, s, plo, phi);
+}
+
 // One CTA of kMaxBlockThreads per SM caps the kernel at 64 registers.
 #ifndef PP_PROPAGATE_MIN_BLOCKS
 #define PP_PROPAGATE_MIN_BLOCKS 1
@@ -362,93 +471,21 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
     const int s = lo;
     const long long p0 = (long long)(c - __ldg(a.chunk_prefix + s)) * a.chunk_photons;
     const long long pend = min(p0 + (long long)a.chunk_photons, __ldg(a.src_photons + s));
-    const pp_source* sp = a.sources + s;
-    const int kind = __ldg(&sp->kind);
-    const float3 spos = make_float3(__ldg(&sp->position[0]), __ldg(&sp->position[1]),
-                                    __ldg(&sp->position[2]));
-    const float3 saxis = make_float3(__ldg(&sp->direction[0]), __ldg(&sp->direction[1]),
-                                     __ldg(&sp->direction[2]));
-    const float stime = __ldg(&sp->time);
-    const long long first = __ldg(&sp->first_photon);
+    const long long first = __ldg(&a.sources[s].first_photon);
 
     for (long long base = p0; base < pend; base += 32) {
       const bool active = base + lane < pend;
       // Lanes past the end replay the first photon of the round (never recorded).
       const long long p = first + (active ? base + lane : base);
       const uint32_t plo = (uint32_t)p, phi = (uint32_t)((unsigned long long)p >> 32);
-      const uint4 r0 = philox(make_uint4(plo, phi, 0u, (uint32_t)s), a.round_keys);
-      const float u0 = u01(r0.x), u1 = u01(r0.y), u2 = u01(r0.z), u3 = u01(r0.w);
-      const float wl = a.spectrum ? spectrum_sample(a.spectrum, a.n_spectrum, u0)
-                                  : a.mono_wavelength;
-      const float4 med = medium_at(a.medium, a.n_medium, a.med_wl_min, a.med_inv_step, wl);
-
-      // ---- initial state (initialize_photon_state) ----
-      float3 pos = spos, dir;
-      float t0 = stime;
-      switch (kind) {
-        case PP_SRC_POINTLIKE_ISOTROPIC:
-        case PP_SRC_POINTLIKE_TIME_RANGE:
-          dir = dir_from_cos<kPrecise>(uniform_ab(-1.0f, 1.0f, u1), u2);
-          if (kind == PP_SRC_POINTLIKE_TIME_RANGE)
-            t0 = uniform_ab(stime, __ldg(&sp->time_end), u3);
-          break;
-        case PP_SRC_COLLIMATED_ISOTROPIC:
-          dir = dir_from_cos<kPrecise>(uniform_ab(__ldg(&sp->cut_angle_cos), 1.0f, u2), u1);
-          break;
-        case PP_SRC_PENCIL: {
-          const float div = __ldg(&sp->beam_divergence);
-          dir = div > 0.0f ? rot_from_ez<kPrecise>(
-                                 saxis, sph_to_cart<kPrecise>(
-                                            f_sqrt<kPrecise>(uniform_ab(0.0f, div * div, u1)), u2))
-                           : saxis;
-          break;
-        }
-        case PP_SRC_AXICONE: {
-          float th = __ldg(&sp->angle);
-          const float div = __ldg(&sp->beam_divergence);
-          if (div > 0.0f) {
-            float cs;
-            if (kPrecise) {
-              cs = cosf(kTwoPi * u3);
-            } else {
-              float sn;
-              f_sincos_2pi<false>(u3, &sn, &cs);
-            }
-            th += f_sqrt<kPrecise>(-2.0f * f_log<kPrecise>(u2)) * cs * div;
-          }
-          dir = rot_from_ez<kPrecise>(saxis, sph_to_cart<kPrecise>(th, u1));
-          break;
-        }
-        case PP_SRC_EXTENDED_CHERENKOV:
-        case PP_SRC_EXTENDED_CHERENKOV_NOSMEAR:
-        case PP_SRC_POINTLIKE_CHERENKOV:
-        case PP_SRC_CHERENKOV_TRACK: {
-          float along = 0.0f;
-          if (kind == PP_SRC_EXTENDED_CHERENKOV || kind == PP_SRC_EXTENDED_CHERENKOV_NOSMEAR) {
-            along = gamma_sample<kPrecise>(__ldg(&sp->long_a), 1.0f / __ldg(&sp->long_b), plo, phi,
-                                           (uint32_t)s, a.key0, a.key1) *
-                    __ldg(&sp->long_lrad);
-          } else if (kind == PP_SRC_CHERENKOV_TRACK) {
-            const uint4 re = philox(make_uint4(plo, phi, kExtraCall, (uint32_t)s), a.round_keys);
-            along = uniform_ab(0.0f, __ldg(&sp->length), u01(re.x));
-          }
-          if (kind != PP_SRC_POINTLIKE_CHERENKOV) {
-            pos = make_float3(spos.x + along * saxis.x, spos.y + along * saxis.y,
-                              spos.z + along * saxis.z);
-            t0 = stime + along / kCVac;
-          }
-          dir = cherenkov_dir<kPrecise>(
-              saxis, med.w, u1, u2, u3, kind != PP_SRC_EXTENDED_CHERENKOV_NOSMEAR,
-              a.track + (size_t)__ldg(&sp->smear_table) * (size_t)a.n_track, a.n_track);
-          break;
-        }
-        default:
-          dir = make_float3(0.0f, 0.0f, 1.0f);
-          break;
+      float3 pos, dir;
+      float sca_len;
+      {
+        const PhotonInit in = init_photon<kPrecise>(a, s, plo, phi);
+        pos = in.pos;
+        dir = in.dir;
+        sca_len = in.med.x;
       }
-
-      const float3 idir = dir;
-      const float sca_len = med.x;
       float dist = 0.0f, comp = 0.0f;  // Kahan-compensated path length
       best.key[lane] = 0xffffffffu;
       __syncwarp();
@@ -555,6 +592,11 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
       int steps_taken = a.n_steps;
       if (active && key != 0xffffffffu) {
         steps_taken = (int)(key >> 16);
+        const PhotonInit in = init_photon_again<kPrecise>(a, s, plo, phi);
+        const float wl = in.wl;
+        const float3 idir = in.dir;
+        const float t0 = in.t0;
+        const float4 med = in.med;
         const float3 hpos = make_float3(best.hx[lane], best.hy[lane], best.hz[lane]);
         const float3 hdir = make_float3(best.ox[lane], best.oy[lane], best.oz[lane]);
         const float hdist = best.dist[lane];
