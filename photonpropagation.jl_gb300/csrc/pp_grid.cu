@@ -370,6 +370,7 @@ int build_safety(const pp_sphere* targets_dev, int n, const GridDev& grid, float
   sg.cell = (float)h;
   sg.inv_cell = (float)(1.0 / h);
   sg.bytes = (uint32_t)(((size_t)sg.n_cells + 15) & ~(size_t)15);
+  sg.set_derived();
   unsigned char* f = nullptr;
   if (cudaMalloc(&f, (size_t)sg.bytes) != cudaSuccess) {
     if (err) *err = "cudaMalloc(safety field) failed";

@@ -45,6 +45,24 @@ struct SafetyDev {
   int dims[3];
   int n_cells;
   uint32_t bytes;  // allocation, n_cells rounded up to 16 (padding bytes are 0)
+  // Derived on the host (set_derived) so that the kernel's tests read them
+  // as constant operands instead of converting dims or re-adding offsets.
+  float fdims[3];  // dims as float
+  float fmaxc[3];  // dims - 1 as float (largest cell coordinate)
+  float lo_sc[3];  // lo * inv_cell
+  float c_lo[3];   // centre of cell 0: lo + cell / 2
+  float bc[3];     // centre of the field's box
+  float he[3];     // half extents of the field's box
+  void set_derived() {
+    for (int a = 0; a < 3; ++a) {
+      fdims[a] = (float)dims[a];
+      fmaxc[a] = (float)(dims[a] - 1);
+      lo_sc[a] = lo[a] * inv_cell;
+      c_lo[a] = lo[a] + 0.5f * cell;
+      bc[a] = 0.5f * (lo[a] + hi[a]);
+      he[a] = 0.5f * (hi[a] - lo[a]);
+    }
+  }
 };
 constexpr float kSafetyQuantum = 0.5f;  // m per uint8 step (saturates at 127.5 m)
 

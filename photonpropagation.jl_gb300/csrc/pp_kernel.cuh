@@ -108,29 +108,41 @@ __device__ bool stage_tables(unsigned char* dst0, const unsigned char* src0, uin
   }
 }
 
+// Field cell nearest to m (clamped to the field): its index, and m's offset
+// from the cell's centre.
+__device__ __forceinline__ int field_cell(const SafetyDev& s, float3 m, float3* off) {
+  const float fx = fminf(fmaxf(floorf(fmaf(m.x, s.inv_cell, -s.lo_sc[0])), 0.0f), s.fmaxc[0]);
+  const float fy = fminf(fmaxf(floorf(fmaf(m.y, s.inv_cell, -s.lo_sc[1])), 0.0f), s.fmaxc[1]);
+  const float fz = fminf(fmaxf(floorf(fmaf(m.z, s.inv_cell, -s.lo_sc[2])), 0.0f), s.fmaxc[2]);
+  *off = make_float3(fmaf(fx, s.cell, s.c_lo[0]) - m.x, fmaf(fy, s.cell, s.c_lo[1]) - m.y,
+                     fmaf(fz, s.cell, s.c_lo[2]) - m.z);
+  return (int)fmaf(fmaf(fz, s.fdims[1], fy), s.fdims[0], fx);
+}
+
+// Stored lower bound of a field cell in metres: the byte b becomes a float
+// through its bit pattern (2^23 + b), exactly.
+template <bool kShared>
+__device__ __forceinline__ float field_value(const unsigned char* __restrict__ f, int idx) {
+  const uint32_t b = kShared ? f[idx] : __ldg(f + idx);
+  return fmaf(__uint_as_float(0x4B000000u | b), kSafetyQuantum, -8388608.0f * kSafetyQuantum);
+}
+
 // True when the safety field proves that no (inflated) target sphere meets
 // the ball of radius R about m.  Branch-free: two lower bounds on the distance
-// from m to every target, of which the larger must exceed R --
-//   the distance from m to the field's box (which contains every target), and
+// from m to every target, of which one must exceed R --
+//   the Chebyshev distance from m to the field's box (which contains every
+//   target; it is below the Euclidean distance), and
 //   D(c) - |m - c| for the centre c of the field cell nearest to m (distance
 //   to the targets is 1-Lipschitz; D(c) is stored quantised down).
 template <bool kShared>
 __device__ __forceinline__ bool ball_clear(const SafetyDev& s, const unsigned char* __restrict__ f,
                                            float3 m, float R) {
-  const float dx = fmaxf(fmaxf(s.lo[0] - m.x, m.x - s.hi[0]), 0.0f);
-  const float dy = fmaxf(fmaxf(s.lo[1] - m.y, m.y - s.hi[1]), 0.0f);
-  const float dz = fmaxf(fmaxf(s.lo[2] - m.z, m.z - s.hi[2]), 0.0f);
-  const float box2 = dx * dx + dy * dy + dz * dz;
-  const float fx = fminf(fmaxf(floorf((m.x - s.lo[0]) * s.inv_cell), 0.0f), (float)(s.dims[0] - 1));
-  const float fy = fminf(fmaxf(floorf((m.y - s.lo[1]) * s.inv_cell), 0.0f), (float)(s.dims[1] - 1));
-  const float fz = fminf(fmaxf(floorf((m.z - s.lo[2]) * s.inv_cell), 0.0f), (float)(s.dims[2] - 1));
-  const int idx = (int)fmaf(fmaf(fz, (float)s.dims[1], fy), (float)s.dims[0], fx);
-  const float D = (float)(kShared ? f[idx] : __ldg(f + idx)) * kSafetyQuantum;
-  const float ox = fmaf(fx + 0.5f, s.cell, s.lo[0]) - m.x;
-  const float oy = fmaf(fy + 0.5f, s.cell, s.lo[1]) - m.y;
-  const float oz = fmaf(fz + 0.5f, s.cell, s.lo[2]) - m.z;
-  const float budget = D - R;
-  return box2 > R * R || (budget > 0.0f && ox * ox + oy * oy + oz * oz < budget * budget);
+  const float box = fmaxf(fmaxf(fabsf(m.x - s.bc[0]) - s.he[0], fabsf(m.y - s.bc[1]) - s.he[1]),
+                          fabsf(m.z - s.bc[2]) - s.he[2]);
+  float3 o;
+  const int idx = field_cell(s, m, &o);
+  const float budget = field_value<kShared>(f, idx) - R;
+  return box > R || (budget > 0.0f && o.x * o.x + o.y * o.y + o.z * o.z < budget * budget);
 }
 
 // The segment pos + t*dir, t in [0, L], provably misses every target: it lies
@@ -151,15 +163,9 @@ __device__ __forceinline__ bool segment_clear(const SafetyDev& s, const unsigned
 template <bool kShared, bool P>
 __device__ __forceinline__ float field_bound(const SafetyDev& s, const unsigned char* __restrict__ f,
                                              float3 m) {
-  const float fx = fminf(fmaxf(floorf((m.x - s.lo[0]) * s.inv_cell), 0.0f), (float)(s.dims[0] - 1));
-  const float fy = fminf(fmaxf(floorf((m.y - s.lo[1]) * s.inv_cell), 0.0f), (float)(s.dims[1] - 1));
-  const float fz = fminf(fmaxf(floorf((m.z - s.lo[2]) * s.inv_cell), 0.0f), (float)(s.dims[2] - 1));
-  const int idx = (int)fmaf(fmaf(fz, (float)s.dims[1], fy), (float)s.dims[0], fx);
-  const float D = (float)(kShared ? f[idx] : __ldg(f + idx)) * kSafetyQuantum;
-  const float ox = fmaf(fx + 0.5f, s.cell, s.lo[0]) - m.x;
-  const float oy = fmaf(fy + 0.5f, s.cell, s.lo[1]) - m.y;
-  const float oz = fmaf(fz + 0.5f, s.cell, s.lo[2]) - m.z;
-  return D - f_sqrt<P>(ox * ox + oy * oy + oz * oz);
+  float3 o;
+  const int idx = field_cell(s, m, &o);
+  return field_value<kShared>(f, idx) - f_sqrt<P>(o.x * o.x + o.y * o.y + o.z * o.z);
 }
 
 // Slack (m) taken off each clipped end: covers the rounding of the traced

@@ -159,6 +159,7 @@ void safety_shape(const pp::GridDev& g, pp::SafetyDev* s) {
   s->cell = (float)h;
   s->inv_cell = (float)(1.0 / h);
   s->bytes = (uint32_t)(((size_t)s->n_cells + 15) & ~(size_t)15);
+  s->set_derived();
 }
 
 // Upper bound of the grid's item count from the host copy of the targets.
