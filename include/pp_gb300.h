@@ -428,6 +428,15 @@ PP_API int pp_mlp_set_adam(pp_mlp* mlp, const float* host_m, const float* host_v
  * kernel's waits set a device flag that pp_mlp_check reports. */
 PP_API int pp_mlp_infer(pp_mlp* mlp, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
                         void* stream);
+/* Diagnostic of the inference kernel's bounded waits (no reference
+ * counterpart): pp_mlp_infer with every wait bounded to wait_ns
+ * (1e3..2e9 ns) and the first weight chunk's barrier armed but its copy not
+ * issued, so that the waits on it run out with nothing of theirs in flight;
+ * the kernel winds down (its own copies awaited, tensor memory freed) and the
+ * call returns PP_ERR_TIMEOUT (flag cleared) when the bounds work.  Waits for
+ * `stream`. */
+PP_API int pp_mlp_debug_infer_timeout(pp_mlp* mlp, const float* d_x, int64_t n, float* d_expect,
+                                      int64_t wait_ns, void* stream);
 /* Synchronises `stream`; PP_ERR_TIMEOUT (and clears the flag) if a
  * tensor-core wait of an earlier MLP kernel gave up. */
 PP_API int pp_mlp_check(pp_mlp* mlp, void* stream);
@@ -553,6 +562,15 @@ PP_API int pp_time_residuals(const pp_hit_record* d_records, int64_t n, const do
                              int32_t n_targets, double t0, double* d_tres, void* stream);
 
 /* ---- diagnostics (no reference counterpart) -------------------------------- */
+
+/* The propagation kernel's one wait, made to run out: one launch on the
+ * context's inputs in which every CTA arms its table-staging barrier but
+ * issues no copy, so that the wait, bounded to wait_ns (1e3..2e9 ns), expires
+ * with nothing in flight; each CTA raises PP_FLAG_TIMEOUT and returns.
+ * Returns PP_ERR_TIMEOUT when the bound works (the context stays usable),
+ * PP_OK if the wait ended some other way.  Needs a sphere list whose tables
+ * are staged in shared memory. */
+PP_API int pp_debug_staging_timeout(pp_ctx* ctx, int64_t wait_ns);
 
 /* Philox4x32-10 on the device: out[4*i..4*i+3] = philox(ctr[i], key), n rows.
  * ctr and out are host arrays. */

@@ -230,6 +230,8 @@ SIGNATURES = {
                                     c_void_p]),
     "pp_mlp_last_loss": (c_int32, [c_void_p, POINTER(c_float)]),
     "pp_mlp_infer": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "pp_mlp_debug_infer_timeout": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_int64,
+                                             c_void_p]),
     "pp_mlp_check": (c_int32, [c_void_p, c_void_p]),
     "pp_mlp_get_adam": (c_int32, [c_void_p, POINTER(c_float), POINTER(c_float), c_int64,
                                   POINTER(c_int64)]),
@@ -250,6 +252,7 @@ SIGNATURES = {
                                     c_void_p, c_void_p]),
     "pp_debug_philox": (c_int32, [POINTER(c_uint32), c_int32, c_uint32, c_uint32,
                                   POINTER(c_uint32)]),
+    "pp_debug_staging_timeout": (c_int32, [c_void_p, c_int64]),
     "pp_measure_fp32_peak": (c_int32, [c_int32, POINTER(c_double)]),
     "pp_grid_info": (c_int32, [c_void_p, POINTER(c_int32), POINTER(c_float), POINTER(c_float),
                                POINTER(c_int64), POINTER(c_int64)]),

@@ -712,6 +712,38 @@ PP_API int pp_launch(pp_ctx* ctx, int64_t seed, int32_t n_steps, pp_hit_record* 
   return rc;
 }
 
+PP_API int pp_debug_staging_timeout(pp_ctx* ctx, int64_t wait_ns) {
+  if (!ctx) return set_error(PP_ERR_INVALID, "null context");
+  int rc = check_ready(ctx);
+  if (rc != PP_OK) return rc;
+  if (wait_ns < 1000 || wait_ns > 2000000000)
+    return set_error(PP_ERR_INVALID, "wait_ns must be in [1e3, 2e9]");
+  if (ctx->total_chunks == 0 || ctx->h_targets.empty() || ctx->n_shapes > 0 ||
+      ctx->tuning.target_loop || !use_smem_grid(ctx))
+    return set_error(PP_ERR_INVALID,
+                     "the staging wait needs sources, a sphere list and tables in shared memory");
+  DeviceScope ds(ctx->device);
+  pp_counters* d_ctr = nullptr;
+  PP_CUDA(cudaMalloc(&d_ctr, sizeof(pp_counters)), "cudaMalloc(counters)");
+  LaunchArgs a = make_args(ctx, 1, 1, nullptr, 0, d_ctr);
+  a.wait_limit_ns = (unsigned long long)wait_ns;
+  a.skip_staging_copies = 1;
+  pp_counters c{};
+  cudaError_t e = cudaMemsetAsync(d_ctr, 0, sizeof(pp_counters), ctx->stream);
+  if (e == cudaSuccess)
+    e = pp::launch_propagate(a, ctx->tuning.block_threads, ctx->tuning.ctas_per_sm,
+                             ctx->tuning.precise_math != 0, true, ctx->num_sms, ctx->stream,
+                             nullptr);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&c, d_ctr, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_ctr);
+  if (e != cudaSuccess) return cuda_error(e, "staging-timeout diagnostic");
+  if (c.err_flags & PP_FLAG_TIMEOUT)
+    return set_error(PP_ERR_TIMEOUT, "a bounded device wait (TMA staging) timed out");
+  return PP_OK;
+}
+
 PP_API int pp_launch_histogram(pp_ctx* ctx, int64_t seed, int32_t n_steps, const float* d_tgeo,
                                float* d_hist, int32_t n_bins, float t_offset, float log_lo,
                                float log_hi, pp_counters* d_counters, void* stream) {

@@ -186,6 +186,7 @@ struct LaunchArgs {
   unsigned long long capacity;
   pp_counters* counters;
   unsigned long long wait_limit_ns;        // bound on the TMA staging wait
+  int skip_staging_copies;                 // diagnostic: arm the barrier, copy nothing
 
   // Histogram mode (hist != nullptr): instead of hit records, every hit adds
   // its absorption weight to hist[s * (bins + 1)] (count) and to bin

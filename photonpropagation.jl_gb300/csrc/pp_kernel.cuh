@@ -75,10 +75,13 @@ __device__ __forceinline__ void bulk_copy(unsigned char* dst, const unsigned cha
 
 // Stage two global tables into shared memory with TMA bulk copies completing
 // on one mbarrier.  Every thread then waits on the barrier's phase 0 for at
-// most limit_ns.  Returns false on timeout.
+// most limit_ns.  Returns false on timeout.  skip_copies (a diagnostic, see
+// pp_debug_staging_timeout) arms the barrier but issues no copy, so that the
+// bounded wait runs out with nothing in flight.
 __device__ bool stage_tables(unsigned char* dst0, const unsigned char* src0, uint32_t bytes0,
                              unsigned char* dst1, const unsigned char* src1, uint32_t bytes1,
-                             unsigned long long* bar, unsigned long long limit_ns) {
+                             unsigned long long* bar, unsigned long long limit_ns,
+                             bool skip_copies) {
   const uint32_t bar_a = smem_addr(bar);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar_a), "r"(1) : "memory");
@@ -90,8 +93,10 @@ __device__ bool stage_tables(unsigned char* dst0, const unsigned char* src0, uin
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_a),
                  "r"(bytes0 + bytes1)
                  : "memory");
-    bulk_copy(dst0, src0, bytes0, bar_a);
-    bulk_copy(dst1, src1, bytes1, bar_a);
+    if (!skip_copies) {
+      bulk_copy(dst0, src0, bytes0, bar_a);
+      bulk_copy(dst1, src1, bytes1, bar_a);
+    }
   }
   const unsigned long long t0 = global_timer_ns();
   while (true) {
@@ -434,7 +439,7 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
   const unsigned char* field;
   if (kSmemGrid) {
     if (!stage_tables(smem, a.blob, a.grid.blob_bytes, smem + a.safety_offset, a.safety,
-                      a.sgrid.bytes, &bar, a.wait_limit_ns)) {
+                      a.sgrid.bytes, &bar, a.wait_limit_ns, a.skip_staging_copies != 0)) {
       atomicOr(&a.counters->err_flags, (unsigned)PP_FLAG_TIMEOUT);
       return;
     }

@@ -490,6 +490,8 @@ struct InferParams {
   float* expect;                    // [n]
   float* pdf;                       // [n x n_bins], may be null
   unsigned* err;
+  unsigned long long wait_ns;       // bound on every mbarrier wait
+  int skip_first_copy;              // diagnostic: chunk 0's barrier armed, no copy
 };
 
 // The sequence of jobs every role walks through in the same order.  A CTA
@@ -652,7 +654,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
         const int rows = l == p.n_layers ? p.out_pad : p.hidden;
         for (int j = 0; j * kChunkK < K; ++j, ++k) {
           const uint32_t slot = k % kRingSlots, use = k / kRingSlots;
-          if (abort_flag || !pptc::mbar_wait(&w_empty[slot], (use & 1) ^ 1, kWaitNs)) {
+          if (abort_flag || !pptc::mbar_wait(&w_empty[slot], (use & 1) ^ 1, p.wait_ns)) {
             ok = false;
             break;
           }
@@ -663,12 +665,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
                            pptc::smem_u32(&w_full[slot])),
                        "r"(bytes)
                        : "memory");
-          asm volatile(
-              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
-              "[%3];" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
-              "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
-              "r"(pptc::smem_u32(&w_full[slot]))
-              : "memory");
+          if (!(p.skip_first_copy && k == 0))
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+                "[%3];" ::"r"(pptc::smem_u32(ring + slot * kSlotBytes)),
+                "l"(p.wpack + p.wpack_off[l] + (size_t)j * rows * kChunkK * 2), "r"(bytes),
+                "r"(pptc::smem_u32(&w_full[slot]))
+                : "memory");
         }
         more = it.next(p);
       }
@@ -676,8 +679,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       // every slot is released (its commit has landed) and every copy has
       // landed before shared memory is given up
       for (uint32_t q = k > kRingSlots ? k - kRingSlots : 0; q < k; ++q) {
-        pptc::mbar_wait(&w_full[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
-        pptc::mbar_wait(&w_empty[q % kRingSlots], (q / kRingSlots) & 1, kWaitNs);
+        pptc::mbar_wait(&w_full[q % kRingSlots], (q / kRingSlots) & 1, p.wait_ns);
+        pptc::mbar_wait(&w_empty[q % kRingSlots], (q / kRingSlots) & 1, p.wait_ns);
       }
     }
     __syncwarp();
@@ -700,7 +703,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       while (more && ok) {
         const int T = it.slot, l = it.layer;
         const int K = l == 0 ? p.in_pad : p.hidden;
-        if (abort_flag || !pptc::mbar_wait(&act_ready[T], jobs[T] & 1, kWaitNs)) {
+        if (abort_flag || !pptc::mbar_wait(&act_ready[T], jobs[T] & 1, p.wait_ns)) {
           ok = false;
           break;
         }
@@ -710,7 +713,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
                                                 (uint32_t)(K / 8) * 128u);
         const uint32_t idesc = l == p.n_layers ? idesc_head : idesc_hidden;
         for (int j = 0; j * kChunkK < K; ++j) {
-          if (!pptc::mbar_wait(&w_full[slot], phase, kWaitNs) || abort_flag) {
+          if (!pptc::mbar_wait(&w_full[slot], phase, p.wait_ns) || abort_flag) {
             ok = false;
             break;
           }
@@ -744,7 +747,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       }
       // everything issued has completed before TMEM and shared memory go away
       pptc::mma_commit(&mma_done);
-      if (!pptc::mbar_wait(&mma_done, 0, kWaitNs)) ok = false;
+      if (!pptc::mbar_wait(&mma_done, 0, p.wait_ns)) ok = false;
       if (!ok) abort_flag = 1;
     }
     __syncwarp();
@@ -783,7 +786,7 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       const __half* bh = p.bias_half + (size_t)l * p.hidden;
       const uint32_t bp0 = head ? 0u : bias_pair(bh, s0, p.hidden, lane);
       const uint32_t bp1 = head ? 0u : bias_pair(bh, s0 + 128, p.hidden, lane);
-      if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, kWaitNs))) {
+      if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, p.wait_ns))) {
         ok = false;
         break;
       }
@@ -1562,8 +1565,8 @@ PP_API int pp_mlp_set_adam(pp_mlp* m, const float* host_m, const float* host_v, 
 // Fused inference: expected count (exp of the clamped log-count output) and
 // the softmax time PDF of n feature rows, one CTA per 128 rows; n is not
 // limited by max_batch.  d_pdf may be null.
-PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
-                        void* stream) {
+static int infer_impl(pp_mlp* m, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
+                      void* stream, unsigned long long wait_ns, int skip_first_copy) {
   if (!m || !d_x || !d_expect || n < 0) return fail(PP_ERR_INVALID, "bad arguments");
   if (m->n_layers + 1 > kMaxLayers) return fail(PP_ERR_INVALID, "too many layers");
   if (n == 0) return PP_OK;
@@ -1594,6 +1597,7 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
     p.off_b[l] = m->off_b[l];
   }
   p.expect = d_expect; p.pdf = d_pdf; p.err = m->err;
+  p.wait_ns = wait_ns; p.skip_first_copy = skip_first_copy;
   if (m->num_sms == 0) {
     e = cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device);
     if (e != cudaSuccess) return cuda_fail(e, "SM count");
@@ -1618,6 +1622,21 @@ PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
   if (e != cudaSuccess) return cuda_fail(e, "infer kernel");
   e = cudaGetLastError();
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "infer kernel");
+}
+
+PP_API int pp_mlp_infer(pp_mlp* m, const float* d_x, int64_t n, float* d_expect, float* d_pdf,
+                        void* stream) {
+  return infer_impl(m, d_x, n, d_expect, d_pdf, stream, kWaitNs, 0);
+}
+
+PP_API int pp_mlp_debug_infer_timeout(pp_mlp* m, const float* d_x, int64_t n, float* d_expect,
+                                      int64_t wait_ns, void* stream) {
+  if (!m || !d_x || !d_expect || n < 1) return fail(PP_ERR_INVALID, "bad arguments");
+  if (wait_ns < 1000 || wait_ns > 2000000000)
+    return fail(PP_ERR_INVALID, "wait_ns must be in [1e3, 2e9]");
+  int rc = infer_impl(m, d_x, n, d_expect, nullptr, stream, (unsigned long long)wait_ns, 1);
+  if (rc != PP_OK) return rc;
+  return check_err(m, (cudaStream_t)stream);
 }
 
 // Device error flag of the tensor-core kernels (timeouts), checked and cleared.

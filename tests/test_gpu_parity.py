@@ -174,6 +174,27 @@ def test_overflow_raises(pp, gpu_ctx):
         pp.propagate_photons(setup, pp.HitBuffers(nh - 1))
 
 
+def test_staging_wait_times_out_and_context_recovers(pp, gpu_ctx):
+    """The kernel's one wait (the TMA staging of the culling tables, bounded by
+    %globaltimer) is made to run out: the diagnostic arms the barrier and
+    issues no copy, with a 1 ms bound.  Every CTA must raise PP_FLAG_TIMEOUT
+    and return, the call must report PP_ERR_TIMEOUT, and the next normal
+    launch on the same context must give the same hits as before."""
+    setup = pp.workloads.c1_setup(photons=200_000, seed=6)
+    rc, cols, nh, nsim = gpu_run(pp, setup)
+    assert rc == 0 and nh > 0
+    ctx = pp.get_context(0)
+    lib = pp._lib.load()
+    rc = lib.pp_debug_staging_timeout(ctx.ptr, 1_000_000)
+    assert rc == pp._lib.PP_ERR_TIMEOUT, (rc, pp._lib.last_error())
+    assert "timed out" in pp._lib.last_error()
+    assert lib.pp_debug_staging_timeout(ctx.ptr, 10) == pp._lib.PP_ERR_INVALID
+    rc2, cols2, nh2, nsim2 = gpu_run(pp, setup)
+    assert rc2 == 0 and nh2 == nh and nsim2 == nsim
+    o1, o2 = np.argsort(cols["photon_index"]), np.argsort(cols2["photon_index"])
+    np.testing.assert_array_equal(cols["position"][o1], cols2["position"][o2])
+
+
 def test_propagate_photons_table(pp, gpu_ctx):
     setup = pp.workloads.c0_setup(300_000)
     t = pp.propagate_photons(setup)

@@ -175,6 +175,33 @@ def test_fused_inference_matches_oracle(pp, gpu_ctx, n, hidden, layers, n_bins):
 
 
 @pytest.mark.gpu
+def test_fused_inference_wait_times_out_and_recovers(pp, gpu_ctx):
+    """The fused inference kernel's bounded waits made to run out: the
+    diagnostic arms the first weight chunk's barrier without issuing its copy
+    and bounds every wait to 5 ms.  The MMA warp's wait on that chunk, the
+    producer's and the epilogue's then expire, the kernel winds down and the
+    call reports PP_ERR_TIMEOUT; the next normal inference on the same network
+    gives the same outputs as before."""
+    torch = pytest.importorskip("torch")
+    mlp = pp.surrogate.MLP(max_batch=256, hidden=256, n_layers=4, n_bins=64, seed=7)
+    n = 1000
+    x = torch.tensor(np.random.default_rng(2).normal(size=(n, 8)).astype(np.float32),
+                     device="cuda")
+    e1 = torch.zeros(n, device="cuda")
+    mlp.infer(x.data_ptr(), n, e1.data_ptr())
+    lib = pp._lib.load()
+    scratch = torch.zeros(n, device="cuda")
+    rc = lib.pp_mlp_debug_infer_timeout(mlp.ptr, x.data_ptr(), n, scratch.data_ptr(), 5_000_000,
+                                        None)
+    assert rc == pp._lib.PP_ERR_TIMEOUT, (rc, pp._lib.last_error())
+    assert lib.pp_mlp_check(mlp.ptr, None) == 0  # the flag was cleared
+    e2 = torch.zeros(n, device="cuda")
+    mlp.infer(x.data_ptr(), n, e2.data_ptr())
+    assert torch.equal(e1, e2)
+    mlp.close()
+
+
+@pytest.mark.gpu
 def test_fused_inference_follows_training(pp, gpu_ctx):
     """The packed inference weights are refreshed after each Adam step."""
     torch = pytest.importorskip("torch")
