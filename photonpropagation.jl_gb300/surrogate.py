@@ -358,6 +358,34 @@ class Expectations:
     audit: dict                 # audit statistics of this batch
 
 
+def calibration(pred, obs, n_groups: int = 10) -> dict:
+    """Calibration of predicted against observed counts over ALL pairs (dim
+    ones included): the pairs are split into n_groups equal groups by
+    predicted count; per group the sums of both, the relative bias
+    sum(obs) / sum(pred) - 1 and the pull (sum(obs) - sum(pred)) /
+    sqrt(sum(pred)).  The MC counts are sums of absorption weights w <= 1, whose
+    variance sum(w^2) is at most the Poisson sum(w), so these pulls are
+    conservative (too small by at most that factor); they ignore the network's
+    own spread."""
+    pred = np.asarray(pred, np.float64)
+    obs = np.asarray(obs, np.float64)
+    order = np.argsort(pred, kind="stable")
+    groups = []
+    for g in np.array_split(order, n_groups):
+        if g.size == 0:
+            continue
+        sp, so = float(pred[g].sum()), float(obs[g].sum())
+        groups.append({"n": int(g.size), "pred_lo": float(pred[g].min()),
+                       "pred_hi": float(pred[g].max()), "sum_pred": sp, "sum_obs": so,
+                       "rel_bias": so / sp - 1.0 if sp > 0 else float("nan"),
+                       "pull": (so - sp) / np.sqrt(sp) if sp > 0 else float("nan")})
+    pulls = [g["pull"] for g in groups if np.isfinite(g["pull"])]
+    biases = [g["rel_bias"] for g in groups if np.isfinite(g["rel_bias"])]
+    return {"groups": groups, "max_abs_pull": float(np.max(np.abs(pulls))) if pulls else None,
+            "max_abs_rel_bias": float(np.max(np.abs(biases))) if biases else None,
+            "total_rel_bias": float(obs.sum() / pred.sum() - 1.0) if pred.sum() > 0 else None}
+
+
 class Surrogate:
     """Module expectations from the trained network, with the plain MC as
     fallback and judge.
@@ -366,7 +394,9 @@ class Surrogate:
     rest, run through the MC at `fallback_photons` per pair.  The audited
     pairs measure the network's error on this batch: relative count error
     where the MC saw at least `min_audit_hits` (so that its own Poisson error
-    is small) and the KS distance of the time PDFs.  If the median count
+    is small), the KS distance of the time PDFs, and the calibration of the
+    counts over every audited pair (deciles of the predicted count, see
+    `calibration`).  If the median count
     error exceeds `max_median_error`, the batch fails its error check and,
     with on_failure="mc", every pair of the batch is answered by the MC."""
 
@@ -437,6 +467,8 @@ class Surrogate:
             pos = np.searchsorted(mc_idx, audit)
             judged = mc_c[pos] >= self.min_audit_hits
             nn_a = counts[audit] / scale
+            if audit.size:
+                stats["calibration"] = calibration(nn_a, mc_c[pos])
             rel = np.abs(nn_a[judged] - mc_c[pos][judged]) / mc_c[pos][judged]
             stats.update({
                 "n_judged": int(judged.sum()),

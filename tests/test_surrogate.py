@@ -184,6 +184,40 @@ def test_surrogate_fallback_and_audit(pp, gpu_ctx, trained):
     np.testing.assert_allclose(r2.counts[nn], 2 * r.counts[nn], rtol=1e-6)
 
 
+def test_calibration_groups(pp):
+    """Host check of the calibration summary: equal groups by prediction,
+    sums, biases and pulls; a calibrated Poisson sample has small pulls, a
+    10% overprediction shows in every group."""
+    s = pp.surrogate
+    rng = np.random.default_rng(4)
+    lam = np.exp(rng.uniform(np.log(0.05), np.log(5e4), 5000))
+    obs = rng.poisson(lam)
+    c = s.calibration(lam, obs)
+    assert len(c["groups"]) == 10 and sum(g["n"] for g in c["groups"]) == 5000
+    assert all(g["pred_lo"] <= g["pred_hi"] for g in c["groups"])
+    assert c["max_abs_pull"] < 4
+    bad = s.calibration(1.1 * lam, obs)
+    assert all(-0.12 < g["rel_bias"] < -0.07 for g in bad["groups"][3:])
+
+
+@pytest.mark.gpu
+def test_surrogate_calibrated_on_all_audited_pairs(pp, gpu_ctx, trained):
+    """Every pair audited (not only the bright ones): in each decile of the
+    predicted count the summed network prediction agrees with the summed
+    1e7-photon MC within 10% or three Poisson standard deviations."""
+    s = pp.surrogate
+    ctx = pp.get_context(0)
+    ev = s.sample_pairs(1500, seed=91)
+    sur = s.Surrogate(trained, table_photons=TABLE_PHOTONS, ctx=ctx, audit_fraction=1.0,
+                      max_median_error=1.0)
+    r = sur.expectations(ev, photons=1e7, seed=8, with_pdf=False)
+    cal = r.audit["calibration"]
+    assert sum(g["n"] for g in cal["groups"]) == r.audit["n_audited"] > 1400
+    for g in cal["groups"]:
+        tol = max(0.10, 3.0 / np.sqrt(max(g["sum_pred"], 1e-9)))
+        assert abs(g["rel_bias"]) < tol, cal
+
+
 @pytest.mark.gpu
 def test_surrogate_failed_audit_falls_back_to_mc(pp, gpu_ctx):
     """An untrained network fails the audit's error check: the whole batch is
