@@ -503,7 +503,15 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
       // warp-uniform queue state: [0, n2) clipped, [n2, n2 + n1) not yet
       int n1 = 0, n2 = 0;
       bool found = false;  // shaped targets: the photon has hit
-      for (int k = 1; k <= a.n_steps; ++k) {
+      // The step loop holds no grid walk: when more than 31 checked entries
+      // wait, it stops before appending step k's entries, the walk below takes
+      // 32 of them, and the loop resumes at step k (recomputing its random
+      // numbers and ball test, which are the same).  At the end of the steps
+      // the same walk takes everything left.
+      int k = 1;
+      while (true) {
+      bool flush = true;
+      for (; k <= a.n_steps; ++k) {
         const uint4 r = philox(make_uint4(plo, phi, (uint32_t)k, (uint32_t)s), a.round_keys);
         const float step = -f_log<kPrecise>(u01(r.x)) * sca_len;
         if constexpr (kShapes) {
@@ -559,8 +567,8 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
             n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.grid, a.sgrid, field, lane);
             n1 = 0;
             if (n2 >= 32) {
-              n2 -= 32;
-              test_queue<kPrecise>(q, best, n2, 32, a.grid, cells, items, sph, lane);
+              flush = false;
+              break;
             }
           }
           if (need) {
@@ -588,14 +596,19 @@ __global__ void __launch_bounds__(kMaxBlockThreads, PP_PROPAGATE_MIN_BLOCKS)
         }
         dir = update_direction<kPrecise>(a.phase, dir, u01(r.y), u01(r.z), u01(r.w));
       }
-      if (!kShapes) {
-        if (n1 > 0) n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.grid, a.sgrid, field, lane);
-        while (n2 > 0) {
-          const int c = n2 < 32 ? n2 : 32;
-          n2 -= c;
-          test_queue<kPrecise>(q, best, n2, c, a.grid, cells, items, sph, lane);
-        }
+      if (kShapes) break;
+      if (flush && n1 > 0) {
+        n2 = check_queue<kSmemGrid, kPrecise>(q, n2, n1, a.grid, a.sgrid, field, lane);
+        n1 = 0;
       }
+      while (n2 > 0) {
+        const int c = n2 < 32 ? n2 : 32;
+        n2 -= c;
+        test_queue<kPrecise>(q, best, n2, c, a.grid, cells, items, sph, lane);
+        if (!flush) break;
+      }
+      if (flush) break;
+      }  // resume the steps after a walk
       __syncwarp();
 
       const uint32_t key = best.key[lane];
