@@ -555,7 +555,7 @@ def bench_detection(pp, torch, local, n=100_000_000, reps=5):
     u = torch.rand(n, device="cuda", generator=g)
     rec[:, 3] = 1.0 / (1.0 / 300.0 - u * (1.0 / 300.0 - 1.0 / 800.0))  # density 1/lambda^2
     del u
-    rec[:, 16] = (mi + 1).to(torch.int32).view(torch.float32)
+    rec[:, 7] = (mi + 1).to(torch.int32).view(torch.float32)  # module_index
     ids = torch.empty(n, dtype=torch.int32, device="cuda")
     qe = torch.empty(n, dtype=torch.float32, device="cuda")
     tg = pp.detection.pmt_targets(targets)
@@ -600,7 +600,7 @@ def bench_detection(pp, torch, local, n=100_000_000, reps=5):
     otargets = [dict(position=x.shape.position, radius=x.shape.radius, kind="pom",
                      active_area=x.pmt_area) for x in targets]
     t0 = time.perf_counter()
-    pmt_oracle.detect(host[:, 0:3], host[:, 3], host[:, 16].view(np.int32), otargets, model_d, 0)
+    pmt_oracle.detect(host[:, 0:3], host[:, 3], host[:, 7].view(np.int32), otargets, model_d, 0)
     cpu_rate = m / (time.perf_counter() - t0)
     del rec, ids, qe, mi
     torch.cuda.empty_cache()

@@ -145,18 +145,19 @@ typedef struct pp_tuning {
  * (src/photon_prop_cuda.jl:407-416) plus the absorption weight that the
  * reference computes on the host (src/processing.jl:32-44). */
 typedef struct pp_hit_record {
+  /* the first 32 bytes hold what the detection step reads (one sector) */
   float position[3];
   float wavelength;
   float direction[3];
+  int32_t module_index;       /* 1-based index into the target list            */
   float dist_travelled;
   float initial_direction[3];
   float abs_weight;           /* exp(-dist_travelled / absorption_length)     */
-  double time;                /* ns (FP64 accumulator)                         */
-  int64_t photon_index;       /* index of the photon within its source         */
-  int32_t module_index;       /* 1-based index into the target list            */
   int32_t n_steps;            /* step (1-based) at which the photon hit        */
   int32_t source_index;       /* 0-based index into the source list            */
   int32_t reserved;
+  double time;                /* ns (FP64 accumulator)                         */
+  int64_t photon_index;       /* index of the photon within its source         */
 } pp_hit_record;
 
 /* Device-side counters of one launch (zeroed by pp_launch / pp_launch_graph). */

@@ -134,11 +134,11 @@ class pp_detection_models(Structure):
 class pp_hit_record(Structure):
     _fields_ = [
         ("position", c_float * 3), ("wavelength", c_float),
-        ("direction", c_float * 3), ("dist_travelled", c_float),
-        ("initial_direction", c_float * 3), ("abs_weight", c_float),
-        ("time", c_double), ("photon_index", c_int64),
-        ("module_index", c_int32), ("n_steps", c_int32), ("source_index", c_int32),
+        ("direction", c_float * 3), ("module_index", c_int32),
+        ("dist_travelled", c_float), ("initial_direction", c_float * 3),
+        ("abs_weight", c_float), ("n_steps", c_int32), ("source_index", c_int32),
         ("reserved", c_int32),
+        ("time", c_double), ("photon_index", c_int64),
     ]
 
 
@@ -165,10 +165,10 @@ assert ctypes.sizeof(pp_counters) == 48
 # Hit-record layout as a numpy structured dtype (for device buffers viewed on the host).
 HIT_RECORD_DTYPE = [
     ("position", "<f4", (3,)), ("wavelength", "<f4"),
-    ("direction", "<f4", (3,)), ("dist_travelled", "<f4"),
-    ("initial_direction", "<f4", (3,)), ("abs_weight", "<f4"),
+    ("direction", "<f4", (3,)), ("module_index", "<i4"),
+    ("dist_travelled", "<f4"), ("initial_direction", "<f4", (3,)),
+    ("abs_weight", "<f4"), ("n_steps", "<i4"), ("source_index", "<i4"), ("reserved", "<i4"),
     ("time", "<f8"), ("photon_index", "<i8"),
-    ("module_index", "<i4"), ("n_steps", "<i4"), ("source_index", "<i4"), ("reserved", "<i4"),
 ]
 
 

@@ -283,7 +283,8 @@ __device__ __forceinline__ void test_queue(WarpQueue& q, WarpBest& b, int base, 
   __syncwarp();
 }
 
-// Append one hit: one atomic per warp for all lanes that record in this pass.
+// Append one hit: one atomic per warp for all lanes that record in this pass;
+// the record is written as five 16-byte stores in pp_hit_record's order.
 __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, float wl, float3 dir,
                                            float dist, float3 idir, float abs_w, double time,
                                            long long photon, int module_index, int n_steps,
@@ -299,11 +300,10 @@ __device__ __forceinline__ void record_hit(const LaunchArgs& a, float3 pos, floa
   if (slot < a.capacity) {
     float4* r = reinterpret_cast<float4*>(a.hits + slot);
     r[0] = make_float4(pos.x, pos.y, pos.z, wl);
-    r[1] = make_float4(dir.x, dir.y, dir.z, dist);
-    r[2] = make_float4(idir.x, idir.y, idir.z, abs_w);
-    reinterpret_cast<double2*>(r)[3] = make_double2(time, __longlong_as_double(photon));
-    r[4] = make_float4(__int_as_float(module_index), __int_as_float(n_steps),
-                       __int_as_float(source_index), 0.0f);
+    r[1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(module_index));
+    r[2] = make_float4(dist, idir.x, idir.y, idir.z);
+    r[3] = make_float4(abs_w, __int_as_float(n_steps), __int_as_float(source_index), 0.0f);
+    reinterpret_cast<double2*>(r)[4] = make_double2(time, __longlong_as_double(photon));
   } else {
     atomicOr(&a.counters->err_flags, (unsigned)PP_FLAG_OVERFLOW);
     *overflowed = true;

@@ -91,8 +91,10 @@ __global__ void __launch_bounds__(256) pmt_kernel(const PmtArgs a) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n;
        i += (long long)gridDim.x * blockDim.x) {
     const float4* r = reinterpret_cast<const float4*>(a.rec + i);
+    // the record's first 32 bytes: position, wavelength; direction, module
     const float4 pw = __ldg(r);
-    const int module = __float_as_int(__ldg(r + 4).x);  // 1-based
+    const float4 dw = __ldg(r + 1);
+    const int module = __float_as_int(dw.w);  // 1-based
     int id = 0;
     float qe = 0.0f;
     if (module >= 1 && module <= a.n_targets) {
@@ -143,7 +145,6 @@ __global__ void __launch_bounds__(256) pmt_kernel(const PmtArgs a) {
         qe = interp0(m.qe_wavelength, m.qe, m.n_qe, pw.w);
       } else if (t.kind == PP_PMT_DOM && a.dom) {
         const pp_dom_model& m = sdom;
-        const float4 dw = __ldg(r + 1);  // direction, dist_travelled
         const float cz = dw.x * m.zenith_axis[0] + dw.y * m.zenith_axis[1] + dw.z * m.zenith_axis[2];
         float poly = 0.0f;
         for (int k = m.n_poly - 1; k >= 0; --k) poly = fmaf(poly, cz, m.poly[k]);
@@ -153,7 +154,6 @@ __global__ void __launch_bounds__(256) pmt_kernel(const PmtArgs a) {
         qe = 1.0f;
       } else if (t.kind == PP_PMT_MULTIPMT && a.mpmt) {
         const pp_multipmt_model& m = smp;
-        const float4 dw = __ldg(r + 1);
         float proj = 0.0f;
         for (int k = 0; k < m.n_pmt; ++k) {
           const float c = dw.x * m.pmt_dir_module[k][0] + dw.y * m.pmt_dir_module[k][1] +

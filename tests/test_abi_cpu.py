@@ -40,8 +40,8 @@ def test_struct_layouts_match_header(pp):
     assert ctypes.sizeof(L.pp_sphere) == 16
     assert ctypes.sizeof(L.pp_hit_record) == 80
     assert ctypes.sizeof(L.pp_counters) == 48
-    assert L.pp_hit_record.time.offset == 48
-    assert L.pp_hit_record.module_index.offset == 64
+    assert L.pp_hit_record.time.offset == 64
+    assert L.pp_hit_record.module_index.offset == 28  # in the first 32-byte sector
     assert L.pp_source.first_photon.offset == 80
     assert np.dtype(L.HIT_RECORD_DTYPE).itemsize == 80
 
