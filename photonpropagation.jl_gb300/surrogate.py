@@ -80,6 +80,51 @@ def pair_features(p: Pairs) -> np.ndarray:
     return x.astype(np.float32)
 
 
+def feature_box(n_spectra: int = 1):
+    """Bounds of pair_features over the training ranges: (lo, hi), 8 each."""
+    ld = (np.log10([D_MIN, D_MAX]) - 1.34) / 0.45
+    lo = np.array([ld[0], -1, 0, -1, -1, -1, -1, 0], np.float64)
+    hi = np.array([ld[1], 1, 1, 1, 1, 1, 1, n_spectra - 1], np.float64)
+    return lo, hi
+
+
+# The fused inference stores hidden activations (and half pre-activations) in
+# IEEE half precision; it converts with saturation, so a magnitude beyond this
+# would be clipped silently.
+F16_ACTIVATION_LIMIT = 32768.0
+
+
+def _silu_interval(zl, zh):
+    """Image of [zl, zh] under SiLU (decreasing below its minimum at
+    z = -1.27846, increasing above)."""
+    def silu(z):
+        return z / (1.0 + np.exp(-np.clip(z, -80, 80)))
+    z_min, v_min = -1.2784645, -0.2784645
+    hi = np.maximum(silu(zl), silu(zh))
+    lo = np.where(zl >= z_min, silu(zl), np.where(zh >= z_min, v_min, silu(zh)))
+    return lo, hi
+
+
+def activation_bound(W, b, lo, hi) -> float:
+    """Largest magnitude any hidden pre-activation or activation of the network
+    (W, b as MLP.unpack gives them) can reach for inputs in the box [lo, hi],
+    by interval arithmetic (midpoint-radius form, exact per layer for a box).
+    Below F16_ACTIVATION_LIMIT, the fused inference cannot saturate for such
+    inputs."""
+    xl, xh = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
+    worst = float(np.max(np.abs(np.concatenate([xl, xh]))))
+    for l in range(len(W) - 1):
+        w = np.asarray(W[l], np.float64)[:, :xl.shape[0]]
+        c, r = 0.5 * (xl + xh), 0.5 * (xh - xl)
+        zc = w @ c + np.asarray(b[l], np.float64)
+        zr = np.abs(w) @ r
+        zl, zh = zc - zr, zc + zr
+        worst = max(worst, float(np.max(np.abs(np.concatenate([zl, zh])))))
+        xl, xh = _silu_interval(zl, zh)
+        worst = max(worst, float(np.max(np.abs(np.concatenate([xl, xh])))))
+    return worst
+
+
 def in_training_range(p: Pairs) -> np.ndarray:
     return (p.distance >= D_MIN) & (p.distance <= D_MAX) & (p.spectrum_id == 0)
 
@@ -209,6 +254,14 @@ class MLP:
         v = np.ascontiguousarray(v, np.float32)
         check(self._lib.pp_mlp_set_params(self.ptr, v.ctypes.data_as(ctypes.POINTER(c_float)),
                                           self.n_params))
+
+    def activation_bound(self, lo=None, hi=None) -> float:
+        """activation_bound of the current parameters over an input box (by
+        default the training features' box)."""
+        if lo is None:
+            lo, hi = feature_box()
+        W, b = self.unpack(self.params())
+        return activation_bound(W, b, lo, hi)
 
     def unpack(self, flat):
         W, b = [], []
@@ -396,7 +449,11 @@ class Surrogate:
     where the MC saw at least `min_audit_hits` (so that its own Poisson error
     is small), the KS distance of the time PDFs, and the calibration of the
     counts over every audited pair (deciles of the predicted count, see
-    `calibration`).  If the median count
+    `calibration`).  The network answers only pairs inside the training
+    ranges, whose features lie in `feature_box()`; if the network's
+    `activation_bound` over that box reaches F16_ACTIVATION_LIMIT (the fused
+    kernel's half-precision activations could saturate), the batch fails its
+    check as well.  If the median count
     error exceeds `max_median_error`, the batch fails its error check and,
     with on_failure="mc", every pair of the batch is answered by the MC."""
 
@@ -486,8 +543,11 @@ class Surrogate:
             if with_pdf:
                 pdf[mc_idx] = self._normalise(mc_h)
             from_mc[mc_idx] = True
+        bound = self.mlp.activation_bound()
+        stats["f16_activation_bound"] = bound
         # no audited pair with enough MC statistics: no evidence against the network
-        failed = bool(stats.get("median_rel_error", 0.0) > self.max_median_error)
+        failed = bool(stats.get("median_rel_error", 0.0) > self.max_median_error
+                      or not bound < F16_ACTIVATION_LIMIT)
         stats["passed"] = not failed
         if failed and self.on_failure == "mc":
             rest = np.flatnonzero(~from_mc)

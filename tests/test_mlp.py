@@ -54,6 +54,29 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         assert gb[l][0] == pytest.approx(num, rel=1e-4, abs=1e-7)
 
 
+def test_activation_bound_encloses_the_network(pp):
+    """The interval bound of the hidden activations over an input box is above
+    everything a forward pass over inputs in the box reaches (corners and
+    random points included), and grows with the weights: the check that keeps
+    the fused kernel's half-precision activations from saturating."""
+    s = pp.surrogate
+    rng = np.random.default_rng(12)
+    sizes = [(64, 16), (64, 64), (64, 64), (9, 64)]
+    W = [rng.normal(0, 1.5 / np.sqrt(c), (r, c)).astype(np.float32) for r, c in sizes]
+    W[0][:, 8:] = 0.0  # padded input columns
+    b = [rng.normal(0, 0.3, r).astype(np.float32) for r, _ in sizes]
+    lo, hi = s.feature_box()
+    corners = np.array([[lo[j] if (k >> j) & 1 else hi[j] for j in range(8)] for k in range(256)])
+    x = np.concatenate([corners, rng.uniform(lo, hi, (20000, 8))])
+    orc = mlp_oracle.MLPOracle(W, b, 8, 8, round_bf16=False)
+    orc.forward(x)
+    reached = max(max(np.abs(z).max() for z in orc.Z), max(np.abs(y).max() for y in orc.Y))
+    bound = s.activation_bound(W, b, lo, hi)
+    assert reached <= bound < np.inf, (reached, bound)
+    big = s.activation_bound([w * 40 for w in W], b, lo, hi)
+    assert big > s.F16_ACTIVATION_LIMIT > bound
+
+
 def test_bf16_rounding_helper():
     x = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 65504.0], np.float32)
     y = mlp_oracle.bf16(x)
