@@ -148,7 +148,15 @@ __device__ __forceinline__ float3 rot_from_ez(float3 a, float3 b) {
     const float sg = a.z >= 0.0f ? 1.0f : -1.0f;
     return make_float3(sg * b.x, sg * b.y, sg * b.z);
   }
-  const float f = a.z >= 0.0f ? f_rcp<P>(1.0f + a.z) : f_div<P>(1.0f - a.z, s2);
+  // 1 / (1 + a.z), written as (1 - a.z) / s2 in the lower hemisphere where
+  // 1 + a.z cancels; the fast form selects the operands of one reciprocal
+  float f;
+  if (P) {
+    f = a.z >= 0.0f ? f_rcp<P>(1.0f + a.z) : f_div<P>(1.0f - a.z, s2);
+  } else {
+    const bool up = a.z >= 0.0f;
+    f = (up ? 1.0f : 1.0f - a.z) * approx_rcp(up ? 1.0f + a.z : s2);
+  }
   const float k = (a.x * b.y - a.y * b.x) * f;
   return make_float3(b.x * a.z + a.x * b.z - a.y * k, b.y * a.z + a.y * b.z + a.x * k,
                      b.z * a.z - (a.x * b.x + a.y * b.y));
