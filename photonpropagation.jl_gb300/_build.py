@@ -24,8 +24,12 @@ INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler",
               "-fPIC,-fvisibility=hidden,-ffp-contract=off", "--expt-relaxed-constexpr"]
-# Per-file flags: the replay kernel must not contract a*b+c into FMAs.
-FILE_FLAGS = {"pp_propagate_precise.cu": ["-fmad=false"]}
+# Per-file flags: no automatic contraction of a*b+c into FMAs in either
+# propagation kernel.  The replay kernel must round as the CPU oracle does; the
+# fast kernel writes its FMAs explicitly, so that every instantiation of the
+# kernel template rounds alike (the culled and the unculled target loop must
+# give the same hits bit for bit).
+FILE_FLAGS = {"pp_propagate_precise.cu": ["-fmad=false"], "pp_propagate.cu": ["-fmad=false"]}
 
 
 def nvcc_path() -> str:

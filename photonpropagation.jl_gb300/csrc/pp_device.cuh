@@ -143,7 +143,7 @@ __device__ __forceinline__ float uniform_ab(float a, float b, float u) { return 
 // hemisphere of a; the expression order matches the oracle's.
 template <bool P>
 __device__ __forceinline__ float3 rot_from_ez(float3 a, float3 b) {
-  const float s2 = a.x * a.x + a.y * a.y;
+  const float s2 = P ? a.x * a.x + a.y * a.y : fmaf(a.y, a.y, a.x * a.x);
   if (s2 == 0.0f) {
     const float sg = a.z >= 0.0f ? 1.0f : -1.0f;
     return make_float3(sg * b.x, sg * b.y, sg * b.z);
@@ -157,9 +157,17 @@ __device__ __forceinline__ float3 rot_from_ez(float3 a, float3 b) {
     const bool up = a.z >= 0.0f;
     f = (up ? 1.0f : 1.0f - a.z) * approx_rcp(up ? 1.0f + a.z : s2);
   }
-  const float k = (a.x * b.y - a.y * b.x) * f;
-  return make_float3(b.x * a.z + a.x * b.z - a.y * k, b.y * a.z + a.y * b.z + a.x * k,
-                     b.z * a.z - (a.x * b.x + a.y * b.y));
+  if (P) {
+    const float k = (a.x * b.y - a.y * b.x) * f;
+    return make_float3(b.x * a.z + a.x * b.z - a.y * k, b.y * a.z + a.y * b.z + a.x * k,
+                       b.z * a.z - (a.x * b.x + a.y * b.y));
+  }
+  // the same with every fused multiply-add written out (the fast variant is
+  // compiled without automatic contraction, so its rounding is fixed here)
+  const float k = fmaf(a.x, b.y, -(a.y * b.x)) * f;
+  return make_float3(fmaf(a.x, b.z, fmaf(b.x, a.z, -(a.y * k))),
+                     fmaf(a.y, b.z, fmaf(b.y, a.z, a.x * k)),
+                     fmaf(b.z, a.z, -fmaf(a.x, b.x, a.y * b.y)));
 }
 
 // sph_to_cart(theta, phi) with phi = 2*pi*u_phi.
@@ -247,8 +255,8 @@ __device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_cho
       other = cbrtf(q + d) + cbrtf(q - d);
     }
   } else {
-    const float t = ph.hg_1mg2 * approx_rcp(fmaf(ph.hg_g, 2.0f * eta - 1.0f, 1.0f));
-    hg = fminf(fmaxf((ph.hg_1pg2 - t * t) * ph.hg_inv2g, -1.0f), 1.0f);
+    const float t = ph.hg_1mg2 * approx_rcp(fmaf(ph.hg_g, fmaf(2.0f, eta, -1.0f), 1.0f));
+    hg = fminf(fmaxf(fmaf(-t, t, ph.hg_1pg2) * ph.hg_inv2g, -1.0f), 1.0f);
     if (ph.kind == PP_PHASE_HG_SL) {
       other = fmaf(2.0f, approx_ex2(ph.sl_exp * approx_lg2(eta)), -1.0f);
     } else {
@@ -260,11 +268,23 @@ __device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_cho
   return u_choice < ph.hg_weight ? hg : other;
 }
 
+// Back onto the unit sphere, for the fast variant: its SFU sine, cosine and
+// square root leave |dir| off 1 by ~1e-6, and the reference's sphere test
+// (b = a^2 - (|p - c|^2 - r^2), which assumes |dir| = 1) turns a norm error e
+// into a shift 2 e a^2 of b -- at 100 m from a module comparable to r^2, and
+// biased: photons then miss distant modules they should hit.  One Newton
+// step of 1/sqrt(n2) from 1 (error ~ (n2 - 1)^2) on the FMA pipe.
+__device__ __forceinline__ float3 renormalise(float3 d) {
+  const float n2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+  const float s = fmaf(-0.5f, n2, 1.5f);
+  return make_float3(d.x * s, d.y * s, d.z * s);
+}
+
 template <bool P>
 __device__ __forceinline__ float3 update_direction(const pp::PhaseDev& ph, float3 dir, float u1,
                                                    float u2, float u3) {
   const float c = scatter_cos<P>(ph, u1, u2);
-  const float s2 = 1.0f - c * c;
+  const float s2 = P ? 1.0f - c * c : fmaf(-c, c, 1.0f);
   const float st = f_sqrt<P>(s2 > 0.0f ? s2 : 0.0f);
   float sp, cp;
   if (P) {
@@ -274,20 +294,29 @@ __device__ __forceinline__ float3 update_direction(const pp::PhaseDev& ph, float
   } else {
     f_sincos_2pi<false>(u3, &sp, &cp);
   }
-  return rot_from_ez<P>(dir, make_float3(cp * st, sp * st, c));
+  const float3 out = rot_from_ez<P>(dir, make_float3(cp * st, sp * st, c));
+  return P ? out : renormalise(out);
 }
 
 // ---- ray-sphere test (_intersect_nsphere, src/photon_prop_cuda.jl:309-343) --
-// Hit iff the near intersection lies strictly inside (0, step).
+// Hit iff the near intersection lies strictly inside (0, step).  Both
+// variants evaluate it exactly as the reference's FP32 expression rounds --
+// no fused multiply-adds, IEEE square root: b = a^2 - (|p - c|^2 - r^2)
+// cancels heavily for distant spheres, so a different rounding order would
+// shift which grazing photons hit (and is not the same everywhere the
+// compiler inlines this); the test runs only in the grid walk, so exactness
+// costs nothing measurable.
 template <bool P>
 __device__ __forceinline__ bool sphere_hit(float4 s, float3 pos, float3 dir, float step,
                                            float* d_out) {
-  const float dx = pos.x - s.x, dy = pos.y - s.y, dz = pos.z - s.z;
-  const float a = dir.x * dx + dir.y * dy + dir.z * dz;
-  const float pp = dx * dx + dy * dy + dz * dz;
-  const float b = a * a - (pp - s.w);
+  const float dx = __fsub_rn(pos.x, s.x), dy = __fsub_rn(pos.y, s.y), dz = __fsub_rn(pos.z, s.z);
+  const float a = __fadd_rn(__fadd_rn(__fmul_rn(dir.x, dx), __fmul_rn(dir.y, dy)),
+                            __fmul_rn(dir.z, dz));
+  const float pp =
+      __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  const float b = __fsub_rn(__fmul_rn(a, a), __fsub_rn(pp, s.w));
   if (b >= 0.0f) {
-    const float d = -a - f_sqrt<P>(b);
+    const float d = __fsub_rn(-a, __fsqrt_rn(b));
     if (d > 0.0f && d < step) {
       *d_out = d;
       return true;

@@ -147,7 +147,7 @@ __device__ __forceinline__ bool ball_clear(const SafetyDev& s, const unsigned ch
   float3 o;
   const int idx = field_cell(s, m, &o);
   const float budget = field_value<kShared>(f, idx) - R;
-  return box > R || (budget > 0.0f && o.x * o.x + o.y * o.y + o.z * o.z < budget * budget);
+  return box > R || (budget > 0.0f && fmaf(o.z, o.z, fmaf(o.y, o.y, o.x * o.x)) < budget * budget);
 }
 
 // The segment pos + t*dir, t in [0, L], provably misses every target: it lies
@@ -158,7 +158,7 @@ __device__ __forceinline__ bool segment_clear(const SafetyDev& s, const unsigned
   const float h = 0.5f * L;
   return ball_clear<kShared>(
       s, f, make_float3(fmaf(dir.x, h, pos.x), fmaf(dir.y, h, pos.y), fmaf(dir.z, h, pos.z)),
-      h * 1.0001f + 1e-4f);
+      fmaf(h, 1.0001f, 1e-4f));
 }
 
 // Lower bound on the distance from m to every (inflated) target sphere:
@@ -170,7 +170,7 @@ __device__ __forceinline__ float field_bound(const SafetyDev& s, const unsigned 
                                              float3 m) {
   float3 o;
   const int idx = field_cell(s, m, &o);
-  return field_value<kShared>(f, idx) - f_sqrt<P>(o.x * o.x + o.y * o.y + o.z * o.z);
+  return field_value<kShared>(f, idx) - f_sqrt<P>(fmaf(o.z, o.z, fmaf(o.y, o.y, o.x * o.x)));
 }
 
 // Slack (m) taken off each clipped end: covers the rounding of the traced
@@ -404,7 +404,7 @@ __device__ __forceinline__ PhotonInit init_photon(const LaunchArgs& a, int s, ui
 
   PhotonInit in;
   in.pos = pos;
-  in.dir = dir;
+  in.dir = kPrecise ? dir : renormalise(dir);
   in.t0 = t0;
   in.wl = wl;
   in.med = med;
