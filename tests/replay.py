@@ -27,9 +27,11 @@ MODES = {
     # replay kernel (IEEE math, no contraction) vs the FP32 oracle
     "precise": dict(rel=1e-5, grazing_cos=0.02, min_match=0.999, max_nongrazing=0.001),
     # fast kernel (SFU approximations): the reference's sqrt(1 - c^2) amplifies
-    # 1-ulp differences of forward scattering cosines, so trajectories agree to
-    # about 1e-3 of the path and a few percent of hits may differ
-    "fast": dict(rel=2e-3, grazing_cos=0.02, min_match=0.95, max_nongrazing=0.05),
+    # 1-ulp differences of forward scattering cosines, so trajectories drift
+    # apart along the path (measured p99 of the relative position error 9e-6
+    # on C0, 1.3e-4 on C1, all within 5e-4) and a few percent of the hits may
+    # differ (C1: 11 one-sided of 310, balanced 6 : 5)
+    "fast": dict(rel=1e-3, grazing_cos=0.02, min_match=0.95, max_nongrazing=0.05),
     # FP32 vs FP64 oracle: the same amplification of FP32 rounding
     "f32_vs_f64": dict(rel=2e-3, grazing_cos=0.02, min_match=0.95, max_nongrazing=0.05),
 }
