@@ -245,7 +245,10 @@ __device__ __forceinline__ int check_queue(WarpQueue& q, int n2, int n1, const G
 }
 
 // Test the checked entries [base, base + c) (c <= 32): lane e walks entry
-// base + e through the grid DDA over its clipped interval; the earliest
+// base + e through the grid DDA over its clipped interval -- or, when at most
+// 16 (10) entries are left, two (three) lanes walk an equal slice of each
+// entry's interval, overlapping by the clip slack, so that the longest walk
+// sets the pass's length less often; the earliest
 // (step, target) per owner lane wins via a shared atomicMin on the key
 // (step << 16 | target), and the winning lane writes the hit state into the
 // owner's slot.
@@ -253,18 +256,25 @@ template <bool P>
 __device__ __forceinline__ void test_queue(WarpQueue& q, WarpBest& b, int base, int c,
                                            const GridDev& g, const uint32_t* cells,
                                            const uint16_t* items, const float4* sph, int lane) {
-  const int e = base + lane;
+  // with few entries, m lanes share one entry, each walking 1/m of its interval
+  const int m = c <= 10 ? 3 : (c <= 16 ? 2 : 1);
+  const int el = lane / m, piece = lane - el * m;
+  const int e = base + el;
   int j = -1, owner = 0;
   uint32_t key = 0;
   float d = 0.0f, d0 = 0.0f;
   float3 p = make_float3(0.0f, 0.0f, 0.0f), dir = p;
-  if (lane < c) {
+  if (el < c) {
     p = make_float3(q.px[e], q.py[e], q.pz[e]);
     dir = make_float3(q.dx[e], q.dy[e], q.dz[e]);
     d0 = q.dist0[e];
     const uint32_t meta = q.meta[e];
     owner = (int)(meta & 31u);
-    j = first_hit<P>(g, cells, items, sph, p, dir, q.len[e], q.t0[e], q.t1[e], &d);
+    const float t0 = q.t0[e], t1 = q.t1[e];
+    const float w = (t1 - t0) * (m == 1 ? 1.0f : (m == 2 ? 0.5f : 0.33333334f));
+    const float ta = piece == 0 ? t0 : fmaxf(fmaf((float)piece, w, t0) - kClipSlack, t0);
+    const float tb = piece == m - 1 ? t1 : fminf(fmaf((float)(piece + 1), w, t0) + kClipSlack, t1);
+    j = first_hit<P>(g, cells, items, sph, p, dir, q.len[e], ta, tb, &d);
     if (j >= 0) {
       key = ((meta >> 8) << 16) | (uint32_t)j;
       atomicMin(&b.key[owner], key);
