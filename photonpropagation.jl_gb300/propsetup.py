@@ -46,6 +46,8 @@ class PhotonPropSetup:
         self.seed = int(seed)
         self.photon_scaling = float(photon_scaling)
         self._track = None if track_smear is None else np.asarray(track_smear, np.float32)
+        self._medium_tables = None  # derived device inputs, computed once
+        self._signature = None
 
     # -- derived device inputs ------------------------------------------------
     def wavelength_range(self):
@@ -54,8 +56,10 @@ class PhotonPropSetup:
         return self.mono_wavelength, self.mono_wavelength
 
     def medium_tables(self):
-        lo, hi = self.wavelength_range()
-        return self.medium.tables(lo, hi, MEDIUM_TABLE_STEP_NM)
+        if self._medium_tables is None:
+            lo, hi = self.wavelength_range()
+            self._medium_tables = self.medium.tables(lo, hi, MEDIUM_TABLE_STEP_NM)
+        return self._medium_tables
 
     def needs_track_smear(self) -> bool:
         return any(s.kind in _sources.TRACK_SMEAR_KINDS for s in self.sources)
@@ -129,28 +133,28 @@ class PhotonPropSetup:
         ctx.uploaded = self.upload_signature(cell_size)
 
     def upload_signature(self, cell_size: float = 0.0):
-        """What `upload` sent: the medium, spectrum and target objects themselves
-        (held, so compared by identity without id reuse) and the derived tables
-        by value.  Media, spectra and targets are taken as immutable once
-        uploaded, as the reference's structs are."""
-        targets = self.targets if isinstance(self.targets, _targets.DetectorLines) \
-            else tuple(self.targets)
-        tables = self.track_table_stack() if self.needs_track_smear() else None
-        return (self.medium, self.spec_dist, targets, self.spectrum_knots, self.mono_wavelength,
-                tables, float(cell_size))
+        """What `upload` sends, by value: the medium tables and phase function,
+        the spectrum knots (or wavelength), the track tables and the target
+        records as bytes, plus the grid cell size.  Two setups with the same
+        detector and medium (say, one per emitter position) then share one
+        upload, as the reference's setups share nothing but upload once each.
+        Computed once per setup: media, spectra and targets are taken as
+        immutable once used, as the reference's structs are."""
+        if self._signature is None:
+            t = self.medium_tables()
+            med = (float(t.wl_min), float(t.wl_step), t.scattering_length.tobytes(),
+                   t.group_velocity.tobytes(), t.absorption_length.tobytes(),
+                   t.phase_refractive_index.tobytes(), float(t.hg_g), float(t.es_b),
+                   float(t.hg_weight), int(t.phase_kind))
+            shaped = self.has_shaped_targets()
+            recs = self.target_records() if shaped else self.sphere_records()
+            knots = None if self.spectrum_knots is None else \
+                np.asarray(self.spectrum_knots, np.float32).tobytes()
+            tables = self.track_table_stack().tobytes() if self.needs_track_smear() else None
+            self._signature = (med, shaped, bytes(memoryview(recs).cast("B")), knots,
+                               self.mono_wavelength, tables)
+        return self._signature + (float(cell_size),)
 
     def is_uploaded(self, ctx, cell_size: float = 0.0) -> bool:
         """True when `ctx` holds exactly what `upload` would send."""
-        cur = getattr(ctx, "uploaded", None)
-        if cur is None:
-            return False
-        new = self.upload_signature(cell_size)
-        same_obj = cur[0] is new[0] and cur[1] is new[1] and (
-            cur[2] is new[2] or (isinstance(cur[2], tuple) and isinstance(new[2], tuple) and
-                                 len(cur[2]) == len(new[2]) and
-                                 all(a is b for a, b in zip(cur[2], new[2]))))
-        def eq(a, b):
-            return (a is None and b is None) or (a is not None and b is not None and
-                                                 np.array_equal(a, b))
-        return same_obj and eq(cur[3], new[3]) and cur[4] == new[4] and eq(cur[5], new[5]) \
-            and cur[6] == new[6]
+        return getattr(ctx, "uploaded", None) == self.upload_signature(cell_size)

@@ -229,4 +229,13 @@ def test_upload_record_follows_the_context(pp):
     c = pp.PhotonPropSetup(list(a.sources), list(t), m, a.spec_dist, 2)
     ctx.uploaded = a.upload_signature()
     assert c.is_uploaded(ctx)  # same objects, another seed: nothing to send
+    # new objects with equal values (another emitter position): nothing to send
+    d = pp.PhotonPropSetup([pp.ExtendedCherenkovEmitter([5, 0, 0], [0, 0, 1.0], 0.0, 10, lp)],
+                           [pp.HomogeneousDetector(pp.Spherical([0.0, 0.0, 10.0], 0.3), 1.0, 1)],
+                           pp.CascadiaMediumProperties(), pp.make_monochromatic_spectrum(450.0), 3)
+    assert d.is_uploaded(ctx)
+    e = pp.PhotonPropSetup(list(a.sources),
+                           [pp.HomogeneousDetector(pp.Spherical([0.0, 0.0, 10.5], 0.3), 1.0, 1)],
+                           m, pp.make_monochromatic_spectrum(450.0), 1)
+    assert not e.is_uploaded(ctx)  # a moved module must be sent
     assert not a.is_uploaded(types.SimpleNamespace(uploaded=None))
