@@ -1032,7 +1032,7 @@ PP_API int pp_autotune(pp_ctx* ctx, int64_t seed, int32_t n_steps, int64_t sampl
     }
     best.cell_size = best_h;
     best_ms = 1e300;
-    const float safety_factors[] = {1.0f, 0.6f};
+    const float safety_factors[] = {1.0f, 0.8f, 0.6f};
     float best_s = auto_s;
     for (float sf : safety_factors) {
       pp_tuning t = best;
