@@ -149,6 +149,53 @@ def test_fast_kernel_hit_rate_unbiased(pp, orc, gpu_ctx):
                                                                             n_f64_only)
 
 
+def _cascades_inside_detector(pp, seed, n_sources=6, photons=1_000_000, rng_seed=19):
+    """Extended Cherenkov cascades (a = 2.0, b = 0.63, lrad = 0.36 m) 3-10 m
+    from modules of the C1 detector, pointing in random directions."""
+    targets, _ = pp.workloads.detector_400()
+    rng = np.random.default_rng(rng_seed)
+    lp = pp.LongitudinalParameterisation(2.0, 0.63, 0.36)
+    srcs = []
+    for _ in range(n_sources):
+        t = np.asarray(targets[rng.integers(len(targets))].shape.position)
+        v = rng.normal(size=3)
+        v *= rng.uniform(3.0, 10.0) / np.linalg.norm(v)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        srcs.append(pp.ExtendedCherenkovEmitter(list(t + v), list(d), 0.0, photons, lp))
+    medium = pp.CascadiaMediumProperties(0.95, 0.2, 1.0, 1.0)
+    spec = pp.make_cherenkov_spectrum((300.0, 800.0), medium)
+    return pp.PhotonPropSetup(srcs, targets, medium, spec, seed)
+
+
+@pytest.mark.gpu
+def test_cascade_emitters_statistics(pp, orc, gpu_ctx):
+    """Cascades among the C1 modules: on the same random streams the fast
+    kernel and the FP64 oracle disagree on as many photons one way as the
+    other (sign test), and on independent streams the per-module counts and
+    the arrival times agree with the FP32 oracle (chi-square, KS; p > 0.01)."""
+    setup = _cascades_inside_detector(pp, seed=71)
+    rc, cols, nh, nsim = gpu_run(pp, setup)
+    assert rc == 0 and nsim == 6 * 1_000_000
+    run = orc.Run.from_setup(setup)
+    keys_f = set(zip(cols["source_index"].tolist(), cols["photon_index"].tolist()))
+    keys_w = set()
+    for src in range(len(setup.sources)):
+        w, _ = run.propagate(src, precision="f64")
+        keys_w |= set(zip(w["source_index"].tolist(), w["photon_index"].tolist()))
+    n_f, n_w = len(keys_f - keys_w), len(keys_w - keys_f)
+    assert n_f + n_w < 0.05 * len(keys_w)
+    assert abs(n_f - n_w) <= 3.0 * np.sqrt(max(n_f + n_w, 1)) + 2, (n_f, n_w)
+    other = _cascades_inside_detector(pp, seed=72)
+    want, _, _ = orc.Run.from_setup(other).propagate_all()
+    n_mod = len(setup.targets)
+    g = np.bincount(cols["module_index"] - 1, minlength=n_mod)
+    o = np.bincount(want["module_index"] - 1, minlength=n_mod)
+    chi2, dof, p = two_sample_poisson_chi2(g, o)
+    assert g.sum() > 1500 and p > P_MIN, (g.sum(), chi2, dof, p)
+    assert stats.ks_2samp(cols["time"], want["time"]).pvalue > P_MIN
+
+
 @pytest.mark.gpu
 def test_c0_arrival_time_histogram(pp, orc, gpu_ctx):
     """The README example (one module at 10 m, 450 nm): the hit count and the
