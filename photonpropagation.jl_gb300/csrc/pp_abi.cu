@@ -104,6 +104,7 @@ struct GraphKey {
 struct pp_ctx {
   int device = 0;
   int num_sms = 0;
+  int chunk_photons = 256;  // photons per queued chunk (build_queue)
   cudaStream_t stream = nullptr;
   // recorded after every launch on the caller's stream: setters wait on it
   // before they overwrite device inputs that a launch in flight still reads
@@ -175,15 +176,24 @@ namespace {
 
 int build_queue(pp_ctx* ctx) {
   const int n = (int)ctx->h_sources.size();
-  const long long chunk = 32LL * ctx->tuning.photons_per_thread;
   std::vector<unsigned long long> prefix(n + 1, 0);
   std::vector<long long> nph(std::max(n, 1), 0);
   long long total = 0;
   for (int i = 0; i < n; ++i) {
     nph[i] = source_photons(ctx->h_sources[i].photons, ctx->scaling);
     total += nph[i];
-    prefix[i + 1] = prefix[i] + (unsigned long long)((nph[i] + chunk - 1) / chunk);
   }
+  // Small workloads: halve the photons per lane and chunk until there are at
+  // least two chunks for every warp the GPU holds at once (32 per SM), so
+  // that a 1e5-photon call is not run by a tenth of the warps.  Photons draw
+  // their random numbers by index, so the chunking changes no result.
+  int ppt = ctx->tuning.photons_per_thread;
+  const long long resident_warps = 32LL * std::max(ctx->num_sms, 1);
+  while (ppt > 1 && total / (32LL * ppt) < 2 * resident_warps) ppt /= 2;
+  const long long chunk = 32LL * ppt;
+  for (int i = 0; i < n; ++i)
+    prefix[i + 1] = prefix[i] + (unsigned long long)((nph[i] + chunk - 1) / chunk);
+  ctx->chunk_photons = (int)chunk;
   if (n > ctx->n_src_alloc) {
     cudaFree(ctx->d_sources);
     cudaFree(ctx->d_prefix);
@@ -277,7 +287,7 @@ LaunchArgs make_args(const pp_ctx* ctx, long long seed, int n_steps, pp_hit_reco
   a.src_photons = ctx->d_src_photons;
   a.total_chunks = ctx->total_chunks;
   a.n_src = ctx->n_src;
-  a.chunk_photons = 32 * ctx->tuning.photons_per_thread;
+  a.chunk_photons = ctx->chunk_photons;
   a.blob = ctx->d_blob;
   a.grid = ctx->grid;
   a.safety = ctx->d_safety;
