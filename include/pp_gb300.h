@@ -423,11 +423,12 @@ PP_API int pp_mlp_set_adam(pp_mlp* mlp, const float* host_m, const float* host_v
 /* Fused inference (one tcgen05 kernel; activations stay in shared memory):
  * d_x (n x n_in, FP32, device) -> d_expect[n] = exp(min(log-count, 30)) and,
  * when d_pdf is not NULL, d_pdf (n x n_bins) = softmax of the time logits.
- * Computed with F16 weights and activations (FP32 accumulation), so hidden
- * activations must stay below 32,768 in magnitude; larger ones are clipped by
- * the saturating conversion without a flag.  The Python layer proves the
- * bound for an input box by interval arithmetic (surrogate.activation_bound)
- * and fails a serving batch whose network could exceed it.
+ * Computed with BF16 weights and activations and FP32 accumulation, the
+ * rounding points of the training forward pass; BF16 keeps FP32's exponent
+ * range, so a finite network cannot saturate.  The Python layer bounds the
+ * hidden activations over an input box by interval arithmetic
+ * (surrogate.activation_bound) and fails a serving batch whose network could
+ * overflow BF16.
  * Asynchronous on `stream`; n is not limited by max_batch.  Timeouts of the
  * kernel's waits set a device flag that pp_mlp_check reports. */
 PP_API int pp_mlp_infer(pp_mlp* mlp, const float* d_x, int64_t n, float* d_expect, float* d_pdf,

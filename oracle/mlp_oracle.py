@@ -4,9 +4,8 @@ numpy restatement of the forward pass, the Poisson + multinomial loss and the
 backward pass of photonpropagation.jl_gb300/csrc/pp_mlp.cu, in FP32 with the
 same BF16 rounding points as the training kernels (inputs, weights, stored
 activations, head gradient, hidden gradients), so that device gradients can be
-checked tensor by tensor; with half=True the forward pass rounds inputs,
-weights and activations to IEEE half, as the fused inference kernel stores
-them.  The surrogate has no counterpart in the reference, so this
+checked tensor by tensor; the fused inference kernel rounds its forward pass
+at the same points.  The surrogate has no counterpart in the reference, so this
 oracle is pinned by finite differences of its own loss (tests/test_mlp.py).
 """
 from __future__ import annotations
@@ -22,11 +21,6 @@ def bf16(x: np.ndarray) -> np.ndarray:
     return u.astype(np.uint32).view(np.float32)
 
 
-def f16(x: np.ndarray) -> np.ndarray:
-    """Round FP32 to IEEE half (nearest even) and back to FP32."""
-    return np.asarray(x, np.float32).astype(np.float16).astype(np.float32)
-
-
 def silu(z):
     return z / (1.0 + np.exp(-z))
 
@@ -39,16 +33,14 @@ def silu_grad(z):
 class MLPOracle:
     """Layers given as lists of padded (W [rows x cols], b [rows]) FP32 arrays."""
 
-    def __init__(self, weights, biases, n_in, n_bins, round_bf16=True, half=False):
-        # round_bf16=False runs everything in FP64 (for finite differences);
-        # half=True rounds at the same points to IEEE half instead, as the
-        # fused inference kernel does
-        self.dtype = np.float32 if round_bf16 or half else np.float64
+    def __init__(self, weights, biases, n_in, n_bins, round_bf16=True):
+        # round_bf16=False runs everything in FP64 (for finite differences)
+        self.dtype = np.float32 if round_bf16 else np.float64
         self.W = [np.asarray(w, self.dtype) for w in weights]
         self.b = [np.asarray(b, self.dtype) for b in biases]
         self.n_in = n_in
         self.n_bins = n_bins
-        self.r = f16 if half else (bf16 if round_bf16 else (lambda a: a))
+        self.r = bf16 if round_bf16 else (lambda a: a)
 
     def forward(self, x):
         r = self.r

@@ -1,6 +1,6 @@
 // pp_mlp.cu -- the learned surrogate: a small MLP trained and evaluated with
-// hand-written tcgen05 kernels (FP32 accumulation in tensor memory): BF16
-// operands for training, F16 for the fused inference kernel.
+// hand-written tcgen05 kernels (BF16 operands, FP32 accumulation in tensor
+// memory) for training and for the fused inference kernel.
 //
 // No counterpart in the reference: PhotonPropagation.jl evaluates an external
 // surrogate (PhotonSurrogateModel, examples/validation.jl:455,673-676) whose
@@ -13,8 +13,8 @@
 // head (1 log-expected-count + 64 time logits, padded to 80).  Loss per sample
 // (Poisson + multinomial negative log-likelihood):
 //   L = exp(o0) - k*o0 - sum_b h_b * log softmax(o_1..64)_b.
-// Parameters are FP32 masters with a BF16 copy for training and an F16 pack
-// for inference; Adam.
+// Parameters are FP32 masters with a BF16 copy for training and a BF16 pack
+// in the tensor core's layout for inference; Adam.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -427,13 +427,14 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, long long n, bf16* _
 // ---------------------------------------------------------------------------
 // Fused inference.
 //
-// The inference network runs in half precision (F16 operands, FP32
-// accumulators): F16 keeps three more mantissa bits than BF16 over the range
-// a trained network's activations take (|activation| < 32,768), and its packed
-// pair arithmetic halves the SFU work of the SiLU epilogue.  Weights are
+// The inference network runs in BF16 (BF16 operands and activations, FP32
+// accumulators and FP32 bias + SiLU), the rounding points of the training
+// forward pass.  BF16 keeps FP32's exponent range, so no activation can
+// overflow.  Weights are
 // packed once per parameter update from the FP32 parameters, the hidden
-// layers' scaled by 1/2 so that the accumulator is z/2 - b/2 (the argument of
-// silu(z) = h + h tanh(h), h = z/2), into K-chunks of kChunkK columns (the
+// layers' scaled by 1/2 (exact in BF16) so that the accumulator is z/2 - b/2
+// (h = z/2 is the argument of silu(z) = h + h tanh(h)), into K-chunks of
+// kChunkK columns (the
 // last chunk of a layer may be 16 wide), each chunk a contiguous block in the
 // tensor core's core-matrix layout: element (r, c) of layer l (rows x cols) at
 //   wpack_off[l] + (c / kChunkK) * rows * kChunkK * 2
@@ -458,13 +459,7 @@ __global__ void repack_kernel(const float* __restrict__ w, int rows, int cols, f
   const int j = c / kChunkK, cc = c % kChunkK;
   const size_t off = (size_t)j * rows * kChunkK * 2 +
                      pptc::core_offset(r, cc >> 3, chunk_width(cols, j)) + (cc & 7) * 2;
-  *reinterpret_cast<__half*>(out + off) = __float2half_rn(w[i] * scale);
-}
-
-// b / 2 of a hidden layer in half precision (the epilogue's bias table).
-__global__ void half_bias_kernel(const float* __restrict__ b, int n, __half* __restrict__ out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = __float2half_rn(0.5f * b[i]);
+  *reinterpret_cast<bf16*>(out + off) = __float2bfloat16_rn(w[i] * scale);
 }
 
 constexpr int kMaxLayers = 17;
@@ -478,13 +473,12 @@ struct InferParams {
   int n_in, in_pad, hidden, n_layers, out_pad, n_bins;
   int n_tiles, n_rounds;
   uint32_t slot_cols;               // TMEM columns per accumulator (power of two >= 32)
-  uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) F16)
+  uint32_t act_bytes;               // one tile's activations (128 x max(in_pad, hidden) BF16)
   uint32_t ring_off;                // shared-memory byte offset of the weight ring
   uint32_t head_bias_off;           // offset of the head's FP32 biases (one-pass head), or 0
   int stage_pdf;                    // PDF rows staged through shared memory
   const unsigned char* wpack;
   long long wpack_off[kMaxLayers];  // bytes, multiples of 512
-  const __half* bias_half;          // hidden layer l: b / 2 at l * hidden
   const float* P;                   // FP32 parameters (the head's biases)
   long long off_b[kMaxLayers];
   float* expect;                    // [n]
@@ -535,8 +529,8 @@ __device__ __forceinline__ void load_unit(const InferParams& p, int tile, int u,
 }
 __device__ __forceinline__ void store_unit(const InferParams& p, unsigned char* act, int u,
                                            const float* xin) {
-  const uint4 v = make_uint4(pptc::f16x2_from(xin[0], xin[1]), pptc::f16x2_from(xin[2], xin[3]),
-                             pptc::f16x2_from(xin[4], xin[5]), pptc::f16x2_from(xin[6], xin[7]));
+  const uint4 v = make_uint4(pptc::bf16x2_from(xin[0], xin[1]), pptc::bf16x2_from(xin[2], xin[3]),
+                             pptc::bf16x2_from(xin[4], xin[5]), pptc::bf16x2_from(xin[6], xin[7]));
   *reinterpret_cast<uint4*>(act + pptc::core_offset(u & 127, u >> 7, p.in_pad)) = v;
 }
 __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* act, int tile,
@@ -548,22 +542,27 @@ __device__ __forceinline__ void pack_input(const InferParams& p, unsigned char* 
   }
 }
 
-// b/2 of columns cb + 2 (lane % 16) and + 1 as a packed pair (0 past the
-// layer's width): the bias operand of silu_slice, loaded before the
+// b/2 of columns cb + 2 (lane % 16) and + 1 in FP32 (0 past the layer's
+// width; halving is exact): the bias operand of silu_slice, loaded before the
 // accumulator wait so that its latency is hidden.
-__device__ __forceinline__ uint32_t bias_pair(const __half* __restrict__ bh, int cb, int hidden,
-                                              int lane) {
+__device__ __forceinline__ float2 bias_pair(const float* __restrict__ b, int cb, int hidden,
+                                            int lane) {
   const int c = cb + 2 * (lane & 15);
-  return c < hidden ? __ldg(reinterpret_cast<const uint32_t*>(bh + c)) : 0u;
+  return c < hidden ? make_float2(0.5f * __ldg(b + c), 0.5f * __ldg(b + c + 1))
+                    : make_float2(0.0f, 0.0f);
 }
 
 // Bias + SiLU of one 32-column slice (columns cb .. cb + 31 of this thread's
-// row) into the F16 activations, in packed pairs: h = acc + b/2 (the
-// accumulator holds z/2 - b/2), silu = h + h tanh(h).  bp is this lane's
-// bias_pair of the slice; pair k is broadcast from lane k.
+// row) into the BF16 activations: h = acc + b/2 (the accumulator holds
+// z/2 - b/2), silu = h + h tanh(h) in FP32, one rounding to BF16 per
+// activation (the rounding point of the training forward pass).  The packed
+// BF16 tanh would save no SFU time (it costs two SFU operations per pair) and
+// runs about one BF16 unit low below |h| = 8, which the cancellation in
+// h (1 + tanh h) turns into a bias on SiLU's negative branch.  bp is this
+// lane's bias_pair of the slice; pair k is broadcast from lane k.
 // kFull: all 32 columns exist (no bound checks, fully interleavable).
 template <bool kFull>
-__device__ __forceinline__ void silu_slice(const uint32_t* v, uint32_t bp, int cb, int hidden,
+__device__ __forceinline__ void silu_slice(const uint32_t* v, float2 bp, int cb, int hidden,
                                            unsigned char* act, int r) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -572,10 +571,9 @@ __device__ __forceinline__ void silu_slice(const uint32_t* v, uint32_t bp, int c
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int i = q * 8 + 2 * j;
-      const uint32_t h = pptc::f16x2_add(
-          pptc::f16x2_from(__uint_as_float(v[i]), __uint_as_float(v[i + 1])),
-          __shfl_sync(0xffffffffu, bp, q * 4 + j));
-      o[j] = pptc::f16x2_fma(h, pptc::f16x2_tanh(h), h);
+      const float h0 = __uint_as_float(v[i]) + __shfl_sync(0xffffffffu, bp.x, q * 4 + j);
+      const float h1 = __uint_as_float(v[i + 1]) + __shfl_sync(0xffffffffu, bp.y, q * 4 + j);
+      o[j] = pptc::bf16x2_from(pptc::silu_half(h0), pptc::silu_half(h1));
     }
     *reinterpret_cast<uint4*>(act + pptc::core_offset(r, (cb >> 3) + q, hidden)) =
         make_uint4(o[0], o[1], o[2], o[3]);
@@ -698,8 +696,8 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       // advance by adding the byte offset / 16 to the start address field
       // (shared addresses < 256 KB: the field never carries)
       const uint64_t b_full = pptc::smem_desc(pptc::smem_u32(ring), 128, (uint32_t)(kChunkK / 8) * 128u);
-      const uint32_t idesc_hidden = pptc::idesc_f16(128, p.hidden);
-      const uint32_t idesc_head = pptc::idesc_f16(128, p.out_pad);
+      const uint32_t idesc_hidden = pptc::idesc_bf16(128, p.hidden);
+      const uint32_t idesc_head = pptc::idesc_bf16(128, p.out_pad);
       while (more && ok) {
         const int T = it.slot, l = it.layer;
         const int K = l == 0 ? p.in_pad : p.hidden;
@@ -776,16 +774,16 @@ __global__ void __launch_bounds__(kInferThreads, 1)
       const int T = it.slot, l = it.layer;
       unsigned char* act = smem + (size_t)T * p.act_bytes;
       // this lane's bias values of the job's two column slices, loaded
-      // before the wait (the inner loops broadcast them by shuffle): FP32
-      // for the head, packed b/2 pairs for a hidden layer
+      // before the wait (the inner loops broadcast them by shuffle): b for
+      // the head, pairs of b/2 for a hidden layer
       const bool head = l == p.n_layers;
       const float* __restrict__ bias = p.P + p.off_b[l];
       const int s0 = cgrp * 32, s1 = (cgrp + 4) * 32;
       const float bl0 = head && s0 + lane < p.out_pad ? __ldg(bias + s0 + lane) : 0.0f;
       const float bl1 = head && s1 + lane < p.out_pad ? __ldg(bias + s1 + lane) : 0.0f;
-      const __half* bh = p.bias_half + (size_t)l * p.hidden;
-      const uint32_t bp0 = head ? 0u : bias_pair(bh, s0, p.hidden, lane);
-      const uint32_t bp1 = head ? 0u : bias_pair(bh, s0 + 128, p.hidden, lane);
+      const float2 bp0 = head ? make_float2(0.0f, 0.0f) : bias_pair(bias, s0, p.hidden, lane);
+      const float2 bp1 =
+          head ? make_float2(0.0f, 0.0f) : bias_pair(bias, s0 + 128, p.hidden, lane);
       if (!epi_all(pptc::mbar_wait(&acc_full[T], jobs[T] & 1, p.wait_ns))) {
         ok = false;
         break;
@@ -803,13 +801,13 @@ __global__ void __launch_bounds__(kInferThreads, 1)
           pptc::tmem_wait();
           // (hidden <= 256: one pass with the preloaded pairs; wider layers
           // load theirs here)
-          const uint32_t b0 = c0 == s0 ? bp0 : bias_pair(bh, c0, p.hidden, lane);
-          const uint32_t b1 = c0 == s0 ? bp1 : bias_pair(bh, c0 + 128, p.hidden, lane);
+          const float2 b0 = c0 == s0 ? bp0 : bias_pair(bias, c0, p.hidden, lane);
+          const float2 b1 = c0 == s0 ? bp1 : bias_pair(bias, c0 + 128, p.hidden, lane);
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             if (h == 1 && !two) break;
             const int cb = c0 + h * 128;
-            const uint32_t bp = h ? b1 : b0;
+            const float2 bp = h ? b1 : b0;
             if (cb + 32 <= p.hidden) silu_slice<true>(v[h], bp, cb, p.hidden, act, r);
             else silu_slice<false>(v[h], bp, cb, p.hidden, act, r);
           }
@@ -1064,8 +1062,7 @@ struct pp_mlp {
   bf16* dZ[2] = {nullptr, nullptr};
   float* loss = nullptr;
   unsigned* err = nullptr;
-  unsigned char* wpack = nullptr;       // F16 weights in core-matrix layout
-  __half* bias_half = nullptr;          // b / 2 of the hidden layers, F16
+  unsigned char* wpack = nullptr;       // BF16 weights in core-matrix layout
   std::vector<long long> wpack_off;     // bytes per layer
   bool pack_dirty = true;
   int num_sms = 0;
@@ -1100,7 +1097,6 @@ void mlp_free(pp_mlp* m) {
   cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16); cudaFree(m->dO32);
   cudaFree(m->dZ[0]); cudaFree(m->dZ[1]); cudaFree(m->loss); cudaFree(m->err);
   cudaFree(m->wpack);
-  cudaFree(m->bias_half);
   cudaFree(m->bx); cudaFree(m->bc); cudaFree(m->bh); cudaFree(m->d_step); cudaFree(m->d_sched);
   if (m->step_graph) cudaGraphExecDestroy(m->step_graph);
   if (m->cap_stream) cudaStreamDestroy(m->cap_stream);
@@ -1208,9 +1204,6 @@ int mlp_repack(pp_mlp* m, cudaStream_t s) {
     repack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         m->P + m->off_w[l], m->rows[l], m->cols[l], hidden ? 0.5f : 1.0f,
         m->wpack + m->wpack_off[l]);
-    if (hidden)
-      half_bias_kernel<<<(unsigned)((m->hidden + 255) / 256), 256, 0, s>>>(
-          m->P + m->off_b[l], m->hidden, m->bias_half + (size_t)l * m->hidden);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "repack weights");
@@ -1219,7 +1212,7 @@ int mlp_repack(pp_mlp* m, cudaStream_t s) {
 }
 
 // Shared memory of infer_kernel: the activations of two tiles (128 rows x
-// max(in_pad, hidden) F16 each, at least the head's reduction arrays), then
+// max(in_pad, hidden) BF16 each, at least the head's reduction arrays), then
 // the weight ring.  The head stages a tile's PDF rows (128 x (n_bins + 1)
 // floats) in that tile's activation buffer when they fit before the
 // reduction arrays at its end.
@@ -1336,7 +1329,6 @@ PP_API int pp_mlp_create(pp_mlp** out, int32_t device, int32_t n_in, int32_t hid
     wbytes += (long long)m->rows[l] * m->cols[l] * 2;  // rows, cols multiples of 16: 512-byte steps
   }
   A((void**)&m->wpack, (size_t)wbytes);
-  A((void**)&m->bias_half, sizeof(__half) * (size_t)n_layers * hidden);
   if (e == cudaSuccess) e = cudaMemcpy(m->P, h.data(), pb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->Mo, 0, pb);
   if (e == cudaSuccess) e = cudaMemset(m->Vo, 0, pb);
@@ -1591,7 +1583,7 @@ static int infer_impl(pp_mlp* m, const float* d_x, int64_t n, float* d_expect, f
   while (p.slot_cols < (uint32_t)std::max(m->hidden, m->out_pad)) p.slot_cols *= 2;
   p.act_bytes = sm.act; p.ring_off = sm.ring_off; p.head_bias_off = sm.head_bias_off;
   p.stage_pdf = sm.stage_pdf ? 1 : 0;
-  p.wpack = m->wpack; p.bias_half = m->bias_half; p.P = m->P;
+  p.wpack = m->wpack; p.P = m->P;
   for (int l = 0; l <= m->n_layers; ++l) {
     p.wpack_off[l] = m->wpack_off[l];
     p.off_b[l] = m->off_b[l];

@@ -49,32 +49,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
          | ((uint32_t)(m >> 4) << 24);  // M >> 4
 }
 
-// The same with F16 A and B.
-__host__ __device__ constexpr uint32_t idesc_f16(int m, int n) {
-  return (1u << 4)                      // D format: F32
-         | ((uint32_t)(n >> 3) << 17)   // N >> 3 (A and B format fields 0: F16)
-         | ((uint32_t)(m >> 4) << 24);  // M >> 4
-}
-
-// Packed half-precision pairs (low half = the first element).
-__device__ __forceinline__ uint32_t f16x2_from(float lo, float hi) {
+// A packed BF16 pair (low half = the first element).  BF16 has FP32's
+// exponent range, so the conversion cannot overflow a finite activation.
+__device__ __forceinline__ uint32_t bf16x2_from(float lo, float hi) {
   uint32_t d;
-  asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
-  return d;
-}
-__device__ __forceinline__ uint32_t f16x2_add(uint32_t a, uint32_t b) {
-  uint32_t d;
-  asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
-  return d;
-}
-__device__ __forceinline__ uint32_t f16x2_fma(uint32_t a, uint32_t b, uint32_t c) {
-  uint32_t d;
-  asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-  return d;
-}
-__device__ __forceinline__ uint32_t f16x2_tanh(uint32_t a) {
-  uint32_t d;
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(d) : "r"(a));
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
   return d;
 }
 

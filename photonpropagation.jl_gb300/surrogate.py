@@ -89,9 +89,9 @@ def feature_box(n_spectra: int = 1):
 
 
 # The fused inference stores hidden activations (and half pre-activations) in
-# IEEE half precision; it converts with saturation, so a magnitude beyond this
-# would be clipped silently.
-F16_ACTIVATION_LIMIT = 32768.0
+# BF16, whose largest finite value is FP32's to 8 bits; a network whose
+# activations could pass it would give infinities.
+BF16_MAX = 3.3895313892515355e38
 
 
 def _silu_interval(zl, zh):
@@ -109,8 +109,7 @@ def activation_bound(W, b, lo, hi) -> float:
     """Largest magnitude any hidden pre-activation or activation of the network
     (W, b as MLP.unpack gives them) can reach for inputs in the box [lo, hi],
     by interval arithmetic (midpoint-radius form, exact per layer for a box).
-    Below F16_ACTIVATION_LIMIT, the fused inference cannot saturate for such
-    inputs."""
+    Below BF16_MAX, the fused inference cannot overflow for such inputs."""
     xl, xh = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
     worst = float(np.max(np.abs(np.concatenate([xl, xh]))))
     for l in range(len(W) - 1):
@@ -451,8 +450,8 @@ class Surrogate:
     counts over every audited pair (deciles of the predicted count, see
     `calibration`).  The network answers only pairs inside the training
     ranges, whose features lie in `feature_box()`; if the network's
-    `activation_bound` over that box reaches F16_ACTIVATION_LIMIT (the fused
-    kernel's half-precision activations could saturate), the batch fails its
+    `activation_bound` over that box reaches BF16_MAX (the fused kernel's
+    BF16 activations could overflow), the batch fails its
     check as well.  If the median count
     error exceeds `max_median_error`, the batch fails its error check and,
     with on_failure="mc", every pair of the batch is answered by the MC."""
@@ -544,10 +543,10 @@ class Surrogate:
                 pdf[mc_idx] = self._normalise(mc_h)
             from_mc[mc_idx] = True
         bound = self.mlp.activation_bound()
-        stats["f16_activation_bound"] = bound
+        stats["activation_bound"] = bound
         # no audited pair with enough MC statistics: no evidence against the network
         failed = bool(stats.get("median_rel_error", 0.0) > self.max_median_error
-                      or not bound < F16_ACTIVATION_LIMIT)
+                      or not bound < BF16_MAX)
         stats["passed"] = not failed
         if failed and self.on_failure == "mc":
             rest = np.flatnonzero(~from_mc)

@@ -201,26 +201,26 @@ def test_calibration_groups(pp):
 
 
 @pytest.mark.gpu
-def test_trained_network_cannot_saturate_half_activations(pp, gpu_ctx, trained):
+def test_trained_network_cannot_overflow_bf16_activations(pp, gpu_ctx, trained):
     """Over the box of training features, the trained network's hidden
-    activations are provably below the half-precision limit of the fused
-    kernel, and the audit reports that bound; a network whose weights are
-    blown up fails the batch's check and is answered by the MC."""
+    activations are provably below the largest BF16 of the fused kernel's
+    activations, and the audit reports that bound; a network whose weights
+    are blown up past it fails the batch's check and is answered by the MC."""
     s = pp.surrogate
     ctx = pp.get_context(0)
     bound = trained.activation_bound()
-    assert bound < s.F16_ACTIVATION_LIMIT, bound
+    assert bound < s.BF16_MAX, bound
     ev = s.sample_pairs(40, seed=17)
     r = s.Surrogate(trained, table_photons=TABLE_PHOTONS, ctx=ctx, audit_fraction=0.0).expectations(
         ev, seed=1, with_pdf=False)
-    assert r.audit["f16_activation_bound"] == pytest.approx(bound) and r.audit["passed"]
+    assert r.audit["activation_bound"] == pytest.approx(bound) and r.audit["passed"]
     blown = s.MLP(max_batch=256, seed=3)
     flat = trained.params()
     W, b = blown.unpack(flat)
     for w in W[:-1]:
-        w *= 30.0
+        w *= 1e12
     blown.set_params(flat)
-    assert blown.activation_bound() >= s.F16_ACTIVATION_LIMIT
+    assert blown.activation_bound() >= s.BF16_MAX
     r2 = s.Surrogate(blown, table_photons=TABLE_PHOTONS, ctx=ctx, audit_fraction=0.0,
                      fallback_photons=100_000).expectations(ev, seed=1, with_pdf=False)
     assert not r2.audit["passed"] and r2.from_mc.all()
