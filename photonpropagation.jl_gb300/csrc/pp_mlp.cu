@@ -34,7 +34,7 @@ namespace {
 
 constexpr int kTileM = 128;   // rows per CTA tile (tcgen05 M)
 constexpr int kKC = 64;       // K columns staged per iteration
-constexpr int kGemmThreads = 128;
+constexpr int kGemmThreads = 256;  // two warps per TMEM lane quarter
 constexpr unsigned long long kWaitNs = 1000000000ull;
 
 enum GemmMode : int {
@@ -78,7 +78,11 @@ __host__ __device__ inline uint32_t tmem_cols_for(int n) {
 // over blockIdx.z and accumulated atomically).  Every K stage of both operands
 // is requested at once with 16-byte cp.async copies straight into the tensor
 // core's core-matrix layout (no register round trip, zero-filled past the
-// edges); the MMAs of a stage are issued as soon as it lands.
+// edges); the MMAs of a stage are issued as soon as it lands.  Eight warps:
+// warps w and w + 4 read TMEM lane quarter w % 4 (rows 32 (w % 4) .. + 31 of
+// the tile) and take alternate 32-column slices of the accumulator, so that
+// two warps per scheduler hide each other's latency in the copy issue and the
+// epilogue.
 //
 // Shared-memory tile of R rows (M or N) x kKC columns of K, 8 x 8 core matrices
 // of 128 bytes, core matrix (r / 8, k / 8) at ((r / 8) * (kKC / 8) + k / 8) * 128:
@@ -90,10 +94,13 @@ __host__ __device__ inline uint32_t tmem_cols_for(int n) {
 // way a 16-byte piece (8 consecutive elements of the contiguous dimension) is
 // one contiguous 16-byte row of a core matrix, and a K step of 16 advances the
 // descriptor by 256 bytes.
+// (A 128 x 64 tile, two CTAs per SM at 96 KB each, measured 8 % slower per
+// training step: per-CTA setup and the re-read A tiles outweigh the overlap.)
 constexpr int kTileN = 128;
-constexpr int kGemmStages = 4;                       // K <= 256 per CTA
-constexpr uint32_t kTileBytes = 128u * kKC * 2u;     // one operand tile of one stage
-constexpr uint32_t kStageBytes = 2u * kTileBytes;
+constexpr int kGemmStages = 4;                          // K <= 256 per CTA
+constexpr uint32_t kTileBytes = kTileM * kKC * 2u;      // the A tile of one stage
+constexpr uint32_t kTileBytesB = kTileN * kKC * 2u;     // the B tile of one stage
+constexpr uint32_t kStageBytes = kTileBytes + kTileBytesB;
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t bytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes)
@@ -190,11 +197,12 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constan
   pptc::fence_after_sync();
 
   if (ok && nk > 0) {
-    const int row = m0 + warp * 32 + lane;
+    const int quarter = warp & 3;
+    const int row = m0 + quarter * 32 + lane;
     const bool row_ok = row < p.M;
-    for (int c0 = 0; c0 < nt; c0 += 32) {
+    for (int c0 = (warp >> 2) * 32; c0 < nt; c0 += 64) {
       float v[32];
-      pptc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      pptc::tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
       if (!row_ok) continue;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -278,72 +286,137 @@ __global__ void pack_input_kernel(const float* __restrict__ x, int n, int n_in, 
 
 // Poisson + multinomial NLL per sample (one warp per sample) and its gradient
 // with respect to the head outputs.
-__global__ void loss_kernel(const float* __restrict__ O, long long ldo, int B,
-                            const float* __restrict__ count, const float* __restrict__ hist,
-                            int nb, float inv_b, float time_weight, bf16* __restrict__ dO16,
-                            float* __restrict__ dO32, long long ldd, int out_pad,
-                            float* __restrict__ loss) {
-  const int warps = blockDim.x >> 5;
-  const int row = blockIdx.x * warps + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (row >= B) return;
-  const float* o = O + (long long)row * ldo;
-  const float o0 = fminf(o[0], 30.0f);
-  const float lam = __expf(o0);
-  const float k = count[row];
-  float mx = -INFINITY;
-  for (int j = lane; j < nb; j += 32) mx = fmaxf(mx, o[1 + j]);
-  for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, s));
-  float se = 0.0f, sh = 0.0f, shx = 0.0f;
-  for (int j = lane; j < nb; j += 32) {
-    const float x = o[1 + j] - mx;
-    const float h = hist[(long long)row * nb + j];
-    se += __expf(x);
-    sh += h;
-    shx += h * x;
-  }
-  for (int s = 16; s > 0; s >>= 1) {
-    se += __shfl_xor_sync(0xffffffffu, se, s);
-    sh += __shfl_xor_sync(0xffffffffu, sh, s);
-    shx += __shfl_xor_sync(0xffffffffu, shx, s);
-  }
-  const float lse = __logf(se);
-  bf16* d16 = dO16 + (long long)row * ldd;
-  float* d32 = dO32 + (long long)row * ldd;
-  for (int j = lane; j < out_pad; j += 32) {
-    float g = 0.0f;
-    if (j == 0) {
-      g = (lam - k) * inv_b;
-    } else if (j <= nb) {
-      const float pj = __expf(o[j] - mx - lse);
-      g = (sh * pj - hist[(long long)row * nb + j - 1]) * inv_b * time_weight;
+// Poisson + multinomial loss of a batch and its gradient with respect to the
+// head's outputs, one warp per row in one pass: the row's logits and
+// histogram stay in registers (bin j = lane + 32 i, n_bins <= kLossBinsPerLane
+// * 32).  Writes dO16 (BF16, every column up to out_pad, zero past the last
+// bin) and adds the rows' sums of the FP32 gradient into gbias (the head's
+// bias gradient) and their losses into *loss, once per block.
+constexpr int kLossBinsPerLane = 8;
+constexpr int kLossWarps = 8;
+__global__ void __launch_bounds__(kLossWarps * 32)
+    loss_kernel(const float* __restrict__ O, long long ldo, int B, const float* __restrict__ count,
+                const float* __restrict__ hist, int nb, float inv_b, float time_weight,
+                bf16* __restrict__ dO16, long long ldd, int out_pad, float* __restrict__ gbias,
+                float* __restrict__ loss) {
+  __shared__ float s_g[kLossWarps][kLossBinsPerLane * 32 + 1];
+  __shared__ float s_loss[kLossWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float gsum[kLossBinsPerLane + 1];  // [i]: column 1 + lane + 32 i; [last]: column 0
+#pragma unroll
+  for (int i = 0; i <= kLossBinsPerLane; ++i) gsum[i] = 0.0f;
+  float lsum = 0.0f;
+  for (int row = blockIdx.x * kLossWarps + warp; row < B; row += gridDim.x * kLossWarps) {
+    const float* o = O + (long long)row * ldo;
+    const float* h = hist + (long long)row * nb;
+    float x[kLossBinsPerLane], hv[kLossBinsPerLane];
+    float mx = -INFINITY;
+#pragma unroll
+    for (int i = 0; i < kLossBinsPerLane; ++i) {
+      const int j = lane + 32 * i;
+      x[i] = j < nb ? __ldg(o + 1 + j) : -INFINITY;
+      hv[i] = j < nb ? __ldg(h + j) : 0.0f;
+      mx = fmaxf(mx, x[i]);
     }
-    d16[j] = __float2bfloat16(g);
-    d32[j] = g;
+    for (int sh = 16; sh > 0; sh >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, sh));
+    float se = 0.0f, hs = 0.0f, hx = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kLossBinsPerLane; ++i) {
+      if (lane + 32 * i < nb) {
+        x[i] -= mx;
+        hs += hv[i];
+        hx += hv[i] * x[i];
+        x[i] = __expf(x[i]);  // from here on the unnormalised probability
+        se += x[i];
+      }
+    }
+    for (int sh = 16; sh > 0; sh >>= 1) {
+      se += __shfl_xor_sync(0xffffffffu, se, sh);
+      hs += __shfl_xor_sync(0xffffffffu, hs, sh);
+      hx += __shfl_xor_sync(0xffffffffu, hx, sh);
+    }
+    const float inv_se = 1.0f / se;
+    const float gw = inv_b * time_weight;
+    bf16* d16 = dO16 + (long long)row * ldd;
+#pragma unroll
+    for (int i = 0; i < kLossBinsPerLane; ++i) {
+      const int col = 1 + lane + 32 * i;
+      if (col < out_pad) {
+        const float g = col - 1 < nb ? (hs * (x[i] * inv_se) - hv[i]) * gw : 0.0f;
+        d16[col] = __float2bfloat16(g);
+        gsum[i] += g;
+      }
+    }
+    if (lane == 0) {
+      const float o0 = fminf(o[0], 30.0f);
+      const float lam = __expf(o0);
+      const float k = count[row];
+      const float g0 = (lam - k) * inv_b;
+      d16[0] = __float2bfloat16(g0);
+      gsum[kLossBinsPerLane] += g0;
+      const float lt = -(hx - hs * __logf(se));
+      lsum += (lam - k * o0 + time_weight * lt) * inv_b;
+    }
   }
+#pragma unroll
+  for (int i = 0; i < kLossBinsPerLane; ++i) s_g[warp][1 + lane + 32 * i] = gsum[i];
   if (lane == 0) {
-    const float lc = lam - k * o0;
-    const float lt = -(shx - sh * lse);
-    atomicAdd(loss, (lc + time_weight * lt) * inv_b);
+    s_g[warp][0] = gsum[kLossBinsPerLane];
+    s_loss[warp] = lsum;
+  }
+  __syncthreads();
+  for (int col = threadIdx.x; col < out_pad; col += blockDim.x) {
+    float t = 0.0f;
+#pragma unroll
+    for (int w = 0; w < kLossWarps; ++w) t += s_g[w][col];
+    atomicAdd(gbias + col, t);
+  }
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+#pragma unroll
+    for (int w = 0; w < kLossWarps; ++w) t += s_loss[w];
+    atomicAdd(loss, t);
   }
 }
 
-// out[c] += sum over rows of X[r][c] (bias gradients).
-template <typename T>
-__global__ void colsum_kernel(const T* __restrict__ X, int rows, int cols, long long ld,
-                              float* __restrict__ out) {
-  const int c = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int ry = threadIdx.x >> 5;
-  float s = 0.0f;
-  if (c < cols)
-    for (int r = blockIdx.y * 8 + ry; r < rows; r += gridDim.y * 8) s += (float)X[(long long)r * ld + c];
-  __shared__ float red[8][33];
-  red[ry][threadIdx.x & 31] = s;
+// out[c] += sum over rows of X[r][c] for the BF16 gradients of a hidden layer
+// (bias gradients): lane l of each warp sums columns 8 l .. 8 l + 7 with
+// 16-byte loads over the warp's rows, the block's warps meet in shared memory
+// and add once per column.  cols <= 256 and a multiple of 8, ld a multiple of
+// 8, X 16-byte aligned.
+constexpr int kColsumWarps = 8;
+__global__ void __launch_bounds__(kColsumWarps * 32)
+    colsum_kernel(const bf16* __restrict__ X, int rows, int cols, long long ld,
+                  float* __restrict__ out) {
+  __shared__ float red[kColsumWarps][257];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = lane * 8;
+  float acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = 0.0f;
+  if (c < cols) {
+    for (int r = blockIdx.x * kColsumWarps + warp; r < rows; r += gridDim.x * kColsumWarps) {
+      union {
+        uint4 u4;
+        __nv_bfloat162 h2[4];
+      } v;
+      v.u4 = __ldg(reinterpret_cast<const uint4*>(X + (long long)r * ld + c));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float2 f = __bfloat1622float2(v.h2[j]);
+        acc[2 * j] += f.x;
+        acc[2 * j + 1] += f.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) red[warp][c + j] = acc[j];
   __syncthreads();
-  if (ry == 0 && c < cols) {
+  for (int col = threadIdx.x; col < cols; col += blockDim.x) {
     float t = 0.0f;
-    for (int i = 0; i < 8; ++i) t += red[i][threadIdx.x & 31];
-    atomicAdd(out + c, t);
+#pragma unroll
+    for (int w = 0; w < kColsumWarps; ++w) t += red[w][col];
+    atomicAdd(out + col, t);
   }
 }
 
@@ -383,7 +456,8 @@ __global__ void adam_dev_kernel(float* __restrict__ w, const float* __restrict__
 }
 
 // The step about to be taken (Adam step t = *step + 1): its cosine step size
-// and bias corrections.
+// and bias corrections, in double and rounded once, as pp_mlp_train_step
+// computes them.
 __global__ void schedule_kernel(const long long* __restrict__ step, long long step0,
                                 long long total, float lr0, float lr1, float b1, float b2,
                                 float* __restrict__ sched) {
@@ -391,8 +465,8 @@ __global__ void schedule_kernel(const long long* __restrict__ step, long long st
   const double frac = total > 1 ? (double)(done - step0) / (double)(total - 1) : 0.0;
   sched[0] = (float)((double)lr1 + 0.5 * ((double)lr0 - (double)lr1) *
                                        (1.0 + cos(3.14159265358979323846 * frac)));
-  sched[1] = 1.0f - powf(b1, (float)(done + 1));
-  sched[2] = 1.0f - powf(b2, (float)(done + 1));
+  sched[1] = (float)(1.0 - pow((double)b1, (double)(done + 1)));
+  sched[2] = (float)(1.0 - pow((double)b2, (double)(done + 1)));
 }
 
 __global__ void step_kernel(long long* step) { *step += 1; }
@@ -1058,7 +1132,6 @@ struct pp_mlp {
   std::vector<bf16*> Z, Y;
   float* O = nullptr;
   bf16* dO16 = nullptr;
-  float* dO32 = nullptr;
   bf16* dZ[2] = {nullptr, nullptr};
   float* loss = nullptr;
   unsigned* err = nullptr;
@@ -1094,7 +1167,7 @@ namespace {
 
 void mlp_free(pp_mlp* m) {
   cudaFree(m->P); cudaFree(m->G); cudaFree(m->Mo); cudaFree(m->Vo); cudaFree(m->P16);
-  cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16); cudaFree(m->dO32);
+  cudaFree(m->X0); cudaFree(m->O); cudaFree(m->dO16);
   cudaFree(m->dZ[0]); cudaFree(m->dZ[1]); cudaFree(m->loss); cudaFree(m->err);
   cudaFree(m->wpack);
   cudaFree(m->bx); cudaFree(m->bc); cudaFree(m->bh); cudaFree(m->d_step); cudaFree(m->d_sched);
@@ -1144,18 +1217,17 @@ int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cu
   if (e == cudaSuccess) e = cudaMemsetAsync(m->loss, 0, sizeof(float), s);
   if (e != cudaSuccess) return cuda_fail(e, "zero gradients");
   const int L = m->n_layers;
-  loss_kernel<<<(B + 7) / 8, 256, 0, s>>>(m->O, m->out_pad, B, d_count, d_hist, m->n_bins,
-                                          1.0f / (float)B, m->time_weight, m->dO16, m->dO32,
-                                          m->out_pad, m->out_pad, m->loss);
+  loss_kernel<<<(unsigned)std::min(256, (B + kLossWarps - 1) / kLossWarps), kLossWarps * 32, 0,
+                s>>>(m->O, m->out_pad, B, d_count, d_hist, m->n_bins, 1.0f / (float)B,
+                     m->time_weight, m->dO16, m->out_pad, m->out_pad, m->G + m->off_b[L],
+                     m->loss);
   const int ksplit = kGemmStages * kKC;
   auto colsum16 = [&](const bf16* X, int cols, long long ld, float* out) {
-    dim3 g((cols + 31) / 32, std::min(64, (B + 7) / 8));
-    colsum_kernel<bf16><<<g, 256, 0, s>>>(X, B, cols, ld, out);
+    const unsigned g = (unsigned)std::min(128, (B + kColsumWarps - 1) / kColsumWarps);
+    colsum_kernel<<<g, kColsumWarps * 32, 0, s>>>(X, B, cols, ld, out);
   };
   // head
   {
-    dim3 g((m->out_pad + 31) / 32, std::min(64, (B + 7) / 8));
-    colsum_kernel<float><<<g, 256, 0, s>>>(m->dO32, B, m->out_pad, m->out_pad, m->G + m->off_b[L]);
     GemmParams p = base_params(m);  // dW_head[o][i] += sum_b dO[b][o] Y[b][i]
     p.A = m->dO16; p.lda = m->out_pad; p.a_trans = 1;
     p.B = m->Y[L - 1]; p.ldb = m->hidden; p.b_trans = 1;
@@ -1318,7 +1390,6 @@ PP_API int pp_mlp_create(pp_mlp** out, int32_t device, int32_t n_in, int32_t hid
   }
   A((void**)&m->O, sizeof(float) * Bn * m->out_pad);
   A((void**)&m->dO16, sizeof(bf16) * Bn * m->out_pad);
-  A((void**)&m->dO32, sizeof(float) * Bn * m->out_pad);
   A((void**)&m->dZ[0], sizeof(bf16) * Bn * hidden);
   A((void**)&m->dZ[1], sizeof(bf16) * Bn * hidden);
   A((void**)&m->loss, sizeof(float));
@@ -1438,8 +1509,12 @@ PP_API int pp_mlp_train_step(pp_mlp* m, const float* d_x, const float* d_count,
   if (rc == PP_OK) rc = mlp_backward(m, d_count, d_hist, B, s);
   if (rc != PP_OK) return rc;
   m->step += 1;
-  const float bc1 = 1.0f - std::pow(m->b1, (float)m->step);
-  const float bc2 = 1.0f - std::pow(m->b2, (float)m->step);
+  // bias corrections in double, rounded once: the captured step's
+  // schedule_kernel computes the same, so that both paths take equal steps
+  // (1 - b2^t cancels, and the float pow of host and device libraries can
+  // differ by an ulp, ~2e-5 of bc2 at small t)
+  const float bc1 = (float)(1.0 - std::pow((double)m->b1, (double)m->step));
+  const float bc2 = (float)(1.0 - std::pow((double)m->b2, (double)m->step));
   adam_kernel<<<(unsigned)((m->n_params + 255) / 256), 256, 0, s>>>(
       m->P, m->G, m->Mo, m->Vo, m->n_params, lr, m->b1, m->b2, m->eps, bc1, bc2, m->P16);
   m->pack_dirty = true;

@@ -304,7 +304,9 @@ def test_train_steps_match_host_loop(pp, gpu_ctx):
     for s in range(steps):
         rows = torch.tensor(_batch_rows(seed, 2 + s + 1, B, n), device="cuda")
         bx, bc, bh = (torch.index_select(t, 0, rows).contiguous() for t in dev)
-        rate = 1e-4 + 0.5 * (2e-3 - 1e-4) * (1.0 + np.cos(np.pi * s / (steps - 1)))
+        # the device schedule's arithmetic: float32 end points, double cosine
+        lr0, lr1 = float(np.float32(2e-3)), float(np.float32(1e-4))
+        rate = lr1 + 0.5 * (lr0 - lr1) * (1.0 + np.cos(np.pi * s / (steps - 1)))
         b.train_step(bx.data_ptr(), bc.data_ptr(), bh.data_ptr(), B, rate)
     torch.cuda.synchronize()
     assert a.step_count() == b.step_count() == steps + 2
