@@ -72,6 +72,18 @@ __host__ __device__ inline uint32_t tmem_cols_for(int n) {
   return c;
 }
 
+// Prologue of every kernel of the training step.  The step's kernels are
+// launched with programmatic stream serialisation (launch_pdl), so a kernel's
+// blocks may be scheduled while its predecessor in the stream still runs:
+// griddepcontrol.wait holds them until the predecessor has completed and its
+// writes are visible (a no-op for a kernel launched without the attribute),
+// and launch_dependents then lets the next kernel be scheduled.  Nothing
+// before pdl_begin may read what an earlier kernel of the stream wrote.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Training GEMM.  One CTA computes a kTileM x (<= kTileN) tile of
 // D = A * B^T over at most kGemmStages * kKC of K (longer reductions are split
@@ -146,6 +158,7 @@ __device__ __forceinline__ void stage_async(uint32_t dst, const bf16* __restrict
 }
 
 __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constant__ GemmParams p) {
+  pdl_begin();
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_slot;
@@ -277,6 +290,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constan
 // Features (n x n_in, FP32) -> zero-padded BF16 rows of in_pad.
 __global__ void pack_input_kernel(const float* __restrict__ x, int n, int n_in, int in_pad,
                                   bf16* __restrict__ out) {
+  pdl_begin();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (long long)n * in_pad) return;
   const long long r = i / in_pad;
@@ -299,6 +313,7 @@ __global__ void __launch_bounds__(kLossWarps * 32)
                 const float* __restrict__ hist, int nb, float inv_b, float time_weight,
                 bf16* __restrict__ dO16, long long ldd, int out_pad, float* __restrict__ gbias,
                 float* __restrict__ loss) {
+  pdl_begin();
   __shared__ float s_g[kLossWarps][kLossBinsPerLane * 32 + 1];
   __shared__ float s_loss[kLossWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -388,6 +403,7 @@ constexpr int kColsumWarps = 8;
 __global__ void __launch_bounds__(kColsumWarps * 32)
     colsum_kernel(const bf16* __restrict__ X, int rows, int cols, long long ld,
                   float* __restrict__ out) {
+  pdl_begin();
   __shared__ float red[kColsumWarps][257];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = lane * 8;
@@ -424,6 +440,7 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
                             float* __restrict__ m, float* __restrict__ v, long long n, float lr,
                             float b1, float b2, float eps, float bc1, float bc2,
                             bf16* __restrict__ w16) {
+  pdl_begin();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float gi = g[i];
@@ -442,6 +459,7 @@ __global__ void adam_dev_kernel(float* __restrict__ w, const float* __restrict__
                                 float* __restrict__ m, float* __restrict__ v, long long n,
                                 const float* __restrict__ sched, float b1, float b2, float eps,
                                 bf16* __restrict__ w16) {
+  pdl_begin();
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float lr = sched[0], bc1 = sched[1], bc2 = sched[2];
@@ -461,6 +479,7 @@ __global__ void adam_dev_kernel(float* __restrict__ w, const float* __restrict__
 __global__ void schedule_kernel(const long long* __restrict__ step, long long step0,
                                 long long total, float lr0, float lr1, float b1, float b2,
                                 float* __restrict__ sched) {
+  pdl_begin();
   const long long done = *step;
   const double frac = total > 1 ? (double)(done - step0) / (double)(total - 1) : 0.0;
   sched[0] = (float)((double)lr1 + 0.5 * ((double)lr0 - (double)lr1) *
@@ -469,7 +488,19 @@ __global__ void schedule_kernel(const long long* __restrict__ step, long long st
   sched[2] = (float)(1.0 - pow((double)b2, (double)(done + 1)));
 }
 
-__global__ void step_kernel(long long* step) { *step += 1; }
+__global__ void step_kernel(long long* step) {
+  pdl_begin();
+  *step += 1;
+}
+
+// Zero the gradient accumulator and the loss (a kernel rather than a memset,
+// so that the step's launches stay one programmatic chain).
+__global__ void zero_kernel(float* __restrict__ g, long long n, float* __restrict__ loss) {
+  pdl_begin();
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) g[i] = 0.0f;
+  if (i == 0) *loss = 0.0f;
+}
 __global__ void set_step_kernel(long long* step, long long v) { *step = v; }
 
 // Batch row i of Adam step t = *step + 1: training row
@@ -480,6 +511,7 @@ __global__ void gather_kernel(const float* __restrict__ x, const float* __restri
                               int n_bins, int B, const long long* __restrict__ step,
                               uint32_t k0, uint32_t k1, float* __restrict__ bx,
                               float* __restrict__ bc, float* __restrict__ bh) {
+  pdl_begin();
   const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (i >= B) return;
@@ -1103,13 +1135,30 @@ cudaError_t gemm_setup() {
   return cudaSuccess;
 }
 
+// Launch with programmatic stream serialisation (the kernel begins with
+// pdl_begin).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 cudaError_t launch_gemm(const GemmParams& p, cudaStream_t s) {
   if (cudaError_t e = gemm_setup()) return e;
   const int splits = (p.K + p.k_per_split - 1) / p.k_per_split;
   const int stages = std::min(kGemmStages, (p.k_per_split + kKC - 1) / kKC);
   dim3 grid((p.M + kTileM - 1) / kTileM, (p.N + kTileN - 1) / kTileN, splits);
-  gemm_kernel<<<grid, kGemmThreads, stages * kStageBytes, s>>>(p);
-  return cudaGetLastError();
+  return launch_pdl(gemm_kernel, grid, dim3(kGemmThreads), stages * kStageBytes, s, p);
 }
 
 inline int pad16(int x) { return (x + 15) & ~15; }
@@ -1185,8 +1234,9 @@ GemmParams base_params(pp_mlp* m) {
 
 int mlp_forward(pp_mlp* m, const float* d_x, int B, cudaStream_t s) {
   const long long nin = (long long)B * m->in_pad;
-  pack_input_kernel<<<(unsigned)((nin + 255) / 256), 256, 0, s>>>(d_x, B, m->n_in, m->in_pad,
-                                                                  m->X0);
+  cudaError_t e0 = launch_pdl(pack_input_kernel, dim3((unsigned)((nin + 255) / 256)), dim3(256), 0,
+                              s, d_x, B, m->n_in, m->in_pad, m->X0);
+  if (e0 != cudaSuccess) return cuda_fail(e0, "pack input");
   const bf16* x = m->X0;
   long long ldx = m->in_pad;
   int kin = m->in_pad;
@@ -1213,18 +1263,19 @@ int mlp_forward(pp_mlp* m, const float* d_x, int B, cudaStream_t s) {
 }
 
 int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(m->G, 0, sizeof(float) * m->n_params, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(m->loss, 0, sizeof(float), s);
+  cudaError_t e = launch_pdl(zero_kernel, dim3((unsigned)((m->n_params + 255) / 256)), dim3(256),
+                             0, s, m->G, m->n_params, m->loss);
   if (e != cudaSuccess) return cuda_fail(e, "zero gradients");
   const int L = m->n_layers;
-  loss_kernel<<<(unsigned)std::min(256, (B + kLossWarps - 1) / kLossWarps), kLossWarps * 32, 0,
-                s>>>(m->O, m->out_pad, B, d_count, d_hist, m->n_bins, 1.0f / (float)B,
-                     m->time_weight, m->dO16, m->out_pad, m->out_pad, m->G + m->off_b[L],
-                     m->loss);
+  e = launch_pdl(loss_kernel, dim3((unsigned)std::min(256, (B + kLossWarps - 1) / kLossWarps)),
+                 dim3(kLossWarps * 32), 0, s, (const float*)m->O, (long long)m->out_pad, B,
+                 d_count, d_hist, m->n_bins, 1.0f / (float)B, m->time_weight, m->dO16,
+                 (long long)m->out_pad, m->out_pad, m->G + m->off_b[L], m->loss);
+  if (e != cudaSuccess) return cuda_fail(e, "loss");
   const int ksplit = kGemmStages * kKC;
   auto colsum16 = [&](const bf16* X, int cols, long long ld, float* out) {
     const unsigned g = (unsigned)std::min(128, (B + kColsumWarps - 1) / kColsumWarps);
-    colsum_kernel<<<g, kColsumWarps * 32, 0, s>>>(X, B, cols, ld, out);
+    return launch_pdl(colsum_kernel, dim3(g), dim3(kColsumWarps * 32), 0, s, X, B, cols, ld, out);
   };
   // head
   {
@@ -1247,7 +1298,8 @@ int mlp_backward(pp_mlp* m, const float* d_count, const float* d_hist, int B, cu
     const bf16* xin = l > 0 ? m->Y[l - 1] : m->X0;
     const long long ldx = l > 0 ? m->hidden : m->in_pad;
     const int nin = l > 0 ? m->hidden : m->in_pad;
-    colsum16(m->dZ[cur], m->hidden, m->hidden, m->G + m->off_b[l]);
+    if ((e = colsum16(m->dZ[cur], m->hidden, m->hidden, m->G + m->off_b[l])) != cudaSuccess)
+      return cuda_fail(e, "bias gradients");
     GemmParams p = base_params(m);  // dW_l[o][i] += sum_b dZ[b][o] x[b][i]
     p.A = m->dZ[cur]; p.lda = m->hidden; p.a_trans = 1;
     p.B = xin; p.ldb = ldx; p.b_trans = 1;
@@ -1515,8 +1567,10 @@ PP_API int pp_mlp_train_step(pp_mlp* m, const float* d_x, const float* d_count,
   // differ by an ulp, ~2e-5 of bc2 at small t)
   const float bc1 = (float)(1.0 - std::pow((double)m->b1, (double)m->step));
   const float bc2 = (float)(1.0 - std::pow((double)m->b2, (double)m->step));
-  adam_kernel<<<(unsigned)((m->n_params + 255) / 256), 256, 0, s>>>(
-      m->P, m->G, m->Mo, m->Vo, m->n_params, lr, m->b1, m->b2, m->eps, bc1, bc2, m->P16);
+  cudaError_t ea = launch_pdl(adam_kernel, dim3((unsigned)((m->n_params + 255) / 256)), dim3(256),
+                              0, s, m->P, (const float*)m->G, m->Mo, m->Vo, m->n_params, lr,
+                              m->b1, m->b2, m->eps, bc1, bc2, m->P16);
+  if (ea != cudaSuccess) return cuda_fail(ea, "adam");
   m->pack_dirty = true;
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? PP_OK : cuda_fail(e, "adam");
@@ -1543,17 +1597,23 @@ int capture_train_step(pp_mlp* m, const pp_mlp::GraphKey& k) {
   cudaStream_t cs = m->cap_stream;
   e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+  // (the first kernel of a step is launched plainly: it follows the previous
+  // graph launch)
   schedule_kernel<<<1, 1, 0, cs>>>(m->d_step, k.step0, k.total, k.lr0, k.lr1, m->b1, m->b2,
                                    m->d_sched);
-  gather_kernel<<<(unsigned)((k.B + 7) / 8), 256, 0, cs>>>(
-      k.x, k.c, k.h, k.n_rows, m->n_in, m->n_bins, k.B, m->d_step, (uint32_t)k.seed,
-      (uint32_t)(k.seed >> 32), m->bx, m->bc, m->bh);
-  int rc = mlp_forward(m, m->bx, k.B, cs);
+  int rc = PP_OK;
+  e = launch_pdl(gather_kernel, dim3((unsigned)((k.B + 7) / 8)), dim3(256), 0, cs, k.x, k.c, k.h,
+                 (long long)k.n_rows, m->n_in, m->n_bins, k.B, (const long long*)m->d_step,
+                 (uint32_t)k.seed, (uint32_t)(k.seed >> 32), m->bx, m->bc, m->bh);
+  if (e != cudaSuccess) rc = cuda_fail(e, "gather");
+  if (rc == PP_OK) rc = mlp_forward(m, m->bx, k.B, cs);
   if (rc == PP_OK) rc = mlp_backward(m, m->bc, m->bh, k.B, cs);
   if (rc == PP_OK) {
-    adam_dev_kernel<<<(unsigned)((m->n_params + 255) / 256), 256, 0, cs>>>(
-        m->P, m->G, m->Mo, m->Vo, m->n_params, m->d_sched, m->b1, m->b2, m->eps, m->P16);
-    step_kernel<<<1, 1, 0, cs>>>(m->d_step);
+    e = launch_pdl(adam_dev_kernel, dim3((unsigned)((m->n_params + 255) / 256)), dim3(256), 0, cs,
+                   m->P, (const float*)m->G, m->Mo, m->Vo, m->n_params, (const float*)m->d_sched,
+                   m->b1, m->b2, m->eps, m->P16);
+    if (e == cudaSuccess) e = launch_pdl(step_kernel, dim3(1), dim3(1), 0, cs, m->d_step);
+    if (e != cudaSuccess) rc = cuda_fail(e, "adam step");
   }
   cudaGraph_t g = nullptr;
   e = cudaStreamEndCapture(cs, &g);  // always end the capture
