@@ -205,15 +205,33 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constan
     }
   }
   if (threadIdx.x == 0) pptc::mma_commit(&bar);
+  // this thread's row, and its (at most two) 32-column slices c0 = 32 (warp / 4)
+  // + 64 si; for the backward dX, the row's saved pre-activations of those
+  // slices are loaded here, while the MMAs run
+  const int quarter = warp & 3;
+  const int row = m0 + quarter * 32 + lane;
+  const bool row_ok = row < p.M;
+  uint4 zpre[2][4];
+  if (p.mode == kBackwardDx && row_ok && nk > 0) {
+#pragma unroll
+    for (int si = 0; si < 2; ++si)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int cc = (warp >> 2) * 32 + si * 64 + q * 8;
+        if (cc < nt)
+          zpre[si][q] =
+              __ldg(reinterpret_cast<const uint4*>(p.Zprev + (long long)row * p.ldzp + n0 + cc));
+      }
+  }
   bool ok = nk > 0 ? pptc::mbar_wait(&bar, 0, kWaitNs) : true;
   ok = __syncthreads_and(ok);
   pptc::fence_after_sync();
 
   if (ok && nk > 0) {
-    const int quarter = warp & 3;
-    const int row = m0 + quarter * 32 + lane;
-    const bool row_ok = row < p.M;
-    for (int c0 = (warp >> 2) * 32; c0 < nt; c0 += 64) {
+#pragma unroll
+    for (int si = 0; si < 2; ++si) {
+      const int c0 = (warp >> 2) * 32 + si * 64;
+      if (c0 >= nt) break;
       float v[32];
       pptc::tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
       if (!row_ok) continue;
@@ -260,7 +278,7 @@ __global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const __grid_constan
               uint4 u4;
               __nv_bfloat162 h2[4];
             } zp, o;
-            zp.u4 = __ldg(reinterpret_cast<const uint4*>(p.Zprev + (long long)row * p.ldzp + col));
+            zp.u4 = zpre[si][q];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
               const float2 z = __bfloat1622float2(zp.h2[j]);
