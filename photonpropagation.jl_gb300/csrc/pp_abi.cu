@@ -116,6 +116,7 @@ struct pp_ctx {
   int n_medium = 0;
   float med_wl_min = 0.0f, med_inv_step = 0.0f;
   pp::PhaseDev phase{};
+  float2* d_es_table = nullptr;  // the phase function's tabulated ES inverse CDF
   bool has_medium = false;
 
   // spectrum
@@ -404,6 +405,7 @@ PP_API int pp_destroy(pp_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   cudaFree(ctx->d_medium);
+  cudaFree(ctx->d_es_table);
   cudaFree(ctx->d_spectrum);
   cudaFree(ctx->d_track);
   cudaFree(ctx->d_targets);
@@ -451,6 +453,17 @@ PP_API int pp_set_medium(pp_ctx* ctx, const pp_medium* m) {
   ctx->n_medium = m->n_knots;
   ctx->med_wl_min = m->wl_min;
   ctx->med_inv_step = 1.0f / m->wl_step;
+  cudaFree(ctx->d_es_table);
+  ctx->d_es_table = nullptr;
+  if (phase.kind == PP_PHASE_HG_ES && m->hg_weight < 1.0f) {
+    std::vector<float2> es(pp::kEsTable);
+    pp::make_es_table(phase.es_b, es.data());
+    PP_CUDA(cudaMalloc(&ctx->d_es_table, sizeof(float2) * es.size()), "cudaMalloc(ES table)");
+    PP_CUDA(cudaMemcpy(ctx->d_es_table, es.data(), sizeof(float2) * es.size(),
+                       cudaMemcpyHostToDevice),
+            "upload ES table");
+  }
+  phase.es_table = ctx->d_es_table;
   ctx->phase = phase;
   ctx->has_medium = true;
   ctx->version++;

@@ -259,6 +259,12 @@ __device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_cho
     hg = fminf(fmaxf(fmaf(-t, t, ph.hg_1pg2) * ph.hg_inv2g, -1.0f), 1.0f);
     if (ph.kind == PP_PHASE_HG_SL) {
       other = fmaf(2.0f, approx_ex2(ph.sl_exp * approx_lg2(eta)), -1.0f);
+    } else if (ph.es_table) {
+      // the tabulated inverse CDF, linearly interpolated (eta in (0, 1])
+      const float x = eta * (float)pp::kEsTable;
+      const int i = min((int)x, pp::kEsTable - 1);
+      const float2 t = __ldg(ph.es_table + i);
+      other = fmaf(x - (float)i, t.y, t.x);
     } else {
       const float q = ph.es_k1 * (eta - 0.5f);
       const float d = approx_sqrt(fmaf(q, q, ph.es_k2));

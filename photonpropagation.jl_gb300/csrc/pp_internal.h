@@ -106,7 +106,32 @@ struct PhaseDev {
   float es_b;       // Einstein-Smoluchowski b
   int kind;         // PP_PHASE_*
   float sl_exp;     // simplified Liu: (1 - g) / (1 + g)
+  // Einstein-Smoluchowski inverse CDF for the fast kernel: kEsTable intervals
+  // of eta on [0, 1], entry i = {q(i / N), q((i + 1) / N) - q(i / N)} (set by
+  // pp_set_medium; null: the Cardano formula)
+  const float2* es_table;
 };
+
+// Intervals of the tabulated Einstein-Smoluchowski inverse CDF.  q(eta) is
+// smooth on [0, 1] (its derivative is 1 / pdf, and pdf ~ 1 + b cos^2 is
+// bounded away from 0), so linear interpolation on 1024 intervals is exact to
+// ~1e-7, below the SFU cube roots of the formula it replaces.
+constexpr int kEsTable = 1024;
+
+// The table of PhaseDev::es_table for parameter b, in double and rounded once:
+// q = cbrt(Q + D) + cbrt(Q - D), Q = (b + 3)(eta - 1/2) / b, D = sqrt(Q^2 + 1/b^3)
+// (the Cardano root of the ES CDF's cubic, as the replay kernel evaluates it).
+inline void make_es_table(float b, float2* out) {
+  const double bb = b, k1 = (bb + 3.0) / bb, k2 = 1.0 / (bb * bb * bb);
+  double prev = 0.0;
+  for (int i = 0; i <= kEsTable; ++i) {
+    const double q = k1 * ((double)i / kEsTable - 0.5);
+    const double d = std::sqrt(q * q + k2);
+    const double v = std::cbrt(q + d) + std::cbrt(q - d);
+    if (i > 0) out[i - 1] = make_float2((float)prev, (float)(v - prev));
+    prev = v;
+  }
+}
 
 // The phase function of a medium, validated: nullptr on success, else the
 // reason.  Shared by pp_set_medium and pp_propagate_static.

@@ -258,9 +258,17 @@ extern "C" PP_API int pp_propagate_static(
       return fail(PP_ERR_INVALID, "medium table entries must be positive");
   }
 
+  // the fast kernel's tabulated ES inverse CDF, as pp_set_medium makes it
+  std::vector<float2> es;
+  if (phase.kind == PP_PHASE_HG_ES && medium->hg_weight < 1.0f) {
+    es.resize(pp::kEsTable);
+    pp::make_es_table(phase.es_b, es.data());
+  }
+
   // ---- carve the scratch ----
   Arena ar{base};
   float4* d_medium = ar.take<float4>(table.size());
+  float2* d_es = ar.take<float2>(std::max<size_t>(es.size(), 1));
   float* d_spec = ar.take<float>(std::max(n_spectrum, 1));
   float* d_track = ar.take<float>(std::max(n_track, 1));
   pp_sphere* d_targets = ar.take<pp_sphere>(std::max(n_targets, 1));
@@ -287,6 +295,7 @@ extern "C" PP_API int pp_propagate_static(
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream) : cudaSuccess;
   };
   cudaError_t e = h2d(d_medium, table.data(), table.size() * sizeof(float4));
+  if (e == cudaSuccess && !es.empty()) e = h2d(d_es, es.data(), es.size() * sizeof(float2));
   if (e == cudaSuccess && n_spectrum > 0) e = h2d(d_spec, spectrum_knots, n_spectrum * sizeof(float));
   if (e == cudaSuccess && n_track > 0 && track_quantiles)
     e = h2d(d_track, track_quantiles, n_track * sizeof(float));
@@ -323,6 +332,7 @@ extern "C" PP_API int pp_propagate_static(
   a.n_medium = medium->n_knots;
   a.med_wl_min = medium->wl_min;
   a.med_inv_step = 1.0f / medium->wl_step;
+  phase.es_table = es.empty() ? nullptr : d_es;
   a.phase = phase;
   a.spectrum = n_spectrum > 0 ? d_spec : nullptr;
   a.n_spectrum = n_spectrum;
