@@ -238,7 +238,9 @@ __device__ __forceinline__ float4 medium_at(const float4* __restrict__ t, int n,
 // CDF) or simplified Liu at g (cos = 2 eta^((1-g)/(1+g)) - 1, the deep-ice
 // mixture).  Both samples are computed and one is selected (a warp almost
 // always needs both anyway); the second component's kind is uniform per
-// launch.
+// launch.  The fast variant reads the Einstein-Smoluchowski root from the
+// medium's table (PhaseDev::es_table) when it has one; the replay variant
+// always evaluates the formula.
 template <bool P>
 __device__ __forceinline__ float scatter_cos(const pp::PhaseDev& ph, float u_choice, float eta) {
   float hg, other;
